@@ -1,0 +1,22 @@
+#!/bin/sh
+# Build oracle/_ref/libqbref.so from the reference's own serial sources
+# (Basis.cc, FourierTransform.cc with its internal FFT_NOLIB transform,
+# UnitCell.cc), compiled in place from the read-only reference tree, plus the
+# one-process Context stub and the C shim in this folder.  The reference's
+# build system is not used.  Test infrastructure only.
+set -e
+REF=${QBG_REFERENCE:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/src/qball/FourierTransform.cc" ]; then
+  echo "build_ref.sh: reference sources not found under $REF; skipping" >&2
+  exit 0
+fi
+mkdir -p "$OUT"
+g++ -O2 -fPIC -shared -std=c++11 -w \
+  -I"$HERE/ref_stub" -I"$REF/src" -I"$REF/src/qball" \
+  "$REF/src/qball/Basis.cc" "$REF/src/qball/FourierTransform.cc" \
+  "$REF/src/qball/UnitCell.cc" \
+  "$HERE/ref_stub/ref_context_stub.cc" "$HERE/ref_shim.cc" \
+  -o "$OUT/libqbref.so"
+echo "built $OUT/libqbref.so"

@@ -1,0 +1,313 @@
+"""ctypes bindings for the CPU oracle (test infrastructure only).
+
+`libqbo.so` (oracle/qbo.c) is the plain-C FP64 restatement of the
+reference's algorithms; `_ref/libqbref.so` is the reference's own serial
+Basis/FourierTransform code compiled from its sources by build_ref.sh (only
+where those sources exist).  Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg import this module, and only as the checker or
+the timed CPU baseline -- the product library never calls into it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_P) if a is not None else None
+
+
+def build():
+    """Compile libqbo.so (and oracle/_ref when the reference tree is present)."""
+    import subprocess
+    subprocess.check_call(["make", "-s", "-C", HERE, "libqbo.so"])
+    subprocess.check_call([os.path.join(HERE, "build_ref.sh")])
+
+
+def _load(name):
+    path = os.path.join(HERE, name)
+    if not os.path.exists(path):
+        raise OSError(f"oracle library {path} not built")
+    return ctypes.CDLL(path)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = _load("libqbo.so")
+        L = _lib
+        L.qbo_basis_dims.argtypes = [_P, _D, _P]
+        L.qbo_basis_fill.argtypes = [_P, _D, _P, _P, _P, _P, _P, _P, _P]
+        L.qbo_cell_volume.argtypes = [_P]
+        L.qbo_cell_volume.restype = _D
+        L.qbo_ft_create.argtypes = [_I, _I, _P, _P, _P, _P, _I, _I, _I, _I]
+        L.qbo_ft_create.restype = _P
+        L.qbo_ft_destroy.argtypes = [_P]
+        L.qbo_ft_backward.argtypes = [_P, _P, _P]
+        L.qbo_ft_forward.argtypes = [_P, _P, _P]
+        L.qbo_ham_create.argtypes = [_P, _I, _P, _D, _P, _I, _P, _P, _P, _P, _P]
+        L.qbo_ham_create.restype = _P
+        L.qbo_ham_destroy.argtypes = [_P]
+        L.qbo_ham_set_A.argtypes = [_P, _P]
+        L.qbo_ham_nproj.argtypes = [_P]
+        L.qbo_ham_projector.argtypes = [_P, _I, _P, _P, _P, _P]
+        L.qbo_hpsi.argtypes = [_P, _P, _I, _I, _P, _P, _I]
+        L.qbo_hpsi.restype = _D
+        L.qbo_nl_apply.argtypes = [_P, _P, _I, _I, _P, _P, _I]
+        L.qbo_nl_apply.restype = _D
+        L.qbo_kinetic_add.argtypes = [_P, _P, _I, _I, _P]
+        L.qbo_rs_mul_add.argtypes = [_P, _P, _I, _I, _P, _I]
+        L.qbo_update_density.argtypes = [_P, _P, _I, _I, _P, _D, _P, _I]
+        L.qbo_update_density.restype = _D
+        L.qbo_current_rs.argtypes = [_P, _P, _I, _P, _I, _I, _P, _D, _P, _D, _P, _I]
+        L.qbo_current_g.argtypes = [_P, _I, _P, _I, _I, _P, _P, _D, _P]
+        L.qbo_etrs_step.argtypes = [_P, _P, _I, _I, _P, _D, _P, _P, _P, _I]
+        L.qbo_etrs_step.restype = _D
+    return _lib
+
+
+def ref():
+    """The reference's own Basis/FourierTransform (None when not built)."""
+    global _ref
+    if _ref is None:
+        try:
+            _ref = _load(os.path.join("_ref", "libqbref.so"))
+        except OSError:
+            return None
+        R = _ref
+        R.qbref_basis_create.argtypes = [_P, _D, _I]
+        R.qbref_basis_create.restype = _P
+        R.qbref_basis_destroy.argtypes = [_P]
+        R.qbref_basis_info.argtypes = [_P, _P]
+        R.qbref_basis_rods.argtypes = [_P, _P, _P, _P, _P]
+        R.qbref_basis_tables.argtypes = [_P, _P, _P, _P]
+        R.qbref_ft_create.argtypes = [_P, _I, _I, _I]
+        R.qbref_ft_create.restype = _P
+        R.qbref_ft_destroy.argtypes = [_P]
+        R.qbref_ft_backward.argtypes = [_P, _P, _P]
+        R.qbref_ft_forward.argtypes = [_P, _P, _P]
+    return _ref
+
+
+class Basis:
+    """Full-sphere plane-wave basis (restated Basis::resize)."""
+
+    def __init__(self, a, ecut, use_ref=False):
+        self.a = np.ascontiguousarray(a, dtype=np.float64).reshape(9)
+        self.ecut = float(ecut)
+        info = np.zeros(12, dtype=np.int32)
+        if use_ref:
+            R = ref()
+            h = R.qbref_basis_create(_ptr(self.a), self.ecut, 1)
+            R.qbref_basis_info(h, _ptr(info))
+        else:
+            lib().qbo_basis_dims(_ptr(self.a), self.ecut, _ptr(info))
+        self.ngw = int(info[0])
+        self.nrods = int(info[1])
+        self.np = tuple(int(x) for x in info[2:5])
+        self.idxmin = tuple(int(x) for x in info[5:8])
+        self.idxmax = tuple(int(x) for x in info[8:11])
+        self.rod_h = np.zeros(self.nrods, np.int32)
+        self.rod_k = np.zeros(self.nrods, np.int32)
+        self.rod_lmin = np.zeros(self.nrods, np.int32)
+        self.rod_size = np.zeros(self.nrods, np.int32)
+        self.idx = np.zeros(3 * self.ngw, np.int32)
+        self.kpg2 = np.zeros(self.ngw)
+        self.kpgx = np.zeros(3 * self.ngw)
+        if use_ref:
+            R.qbref_basis_rods(h, _ptr(self.rod_h), _ptr(self.rod_k),
+                               _ptr(self.rod_lmin), _ptr(self.rod_size))
+            R.qbref_basis_tables(h, _ptr(self.idx), _ptr(self.kpg2), _ptr(self.kpgx))
+            R.qbref_basis_destroy(h)
+        else:
+            lib().qbo_basis_fill(_ptr(self.a), self.ecut, _ptr(self.rod_h), _ptr(self.rod_k),
+                                 _ptr(self.rod_lmin), _ptr(self.rod_size), _ptr(self.idx),
+                                 _ptr(self.kpg2), _ptr(self.kpgx))
+        self.omega = float(lib().qbo_cell_volume(_ptr(self.a)))
+
+    @property
+    def ntrans0(self):
+        return max(abs(self.idxmax[1]), abs(self.idxmin[1])) + 1
+
+
+class FT:
+    """Restated FourierTransform (complex basis, one process)."""
+
+    def __init__(self, basis, np0, np1, np2):
+        self.basis = basis
+        self.shape = (np0, np1, np2)
+        self.n012 = np0 * np1 * np2
+        self.h = lib().qbo_ft_create(basis.ngw, basis.nrods, _ptr(basis.rod_h),
+                                     _ptr(basis.rod_k), _ptr(basis.rod_lmin),
+                                     _ptr(basis.rod_size), np0, np1, np2, basis.ntrans0)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().qbo_ft_destroy(self.h)
+            self.h = None
+
+    def backward(self, c):
+        c = np.ascontiguousarray(c, dtype=np.complex128)
+        f = np.zeros(self.n012, np.complex128)
+        lib().qbo_ft_backward(self.h, _ptr(c), _ptr(f))
+        return f
+
+    def forward(self, f):
+        f = np.array(f, dtype=np.complex128, copy=True)
+        c = np.zeros(self.basis.ngw, np.complex128)
+        lib().qbo_ft_forward(self.h, _ptr(f), _ptr(c))
+        return c
+
+
+class RefFT:
+    """The reference's own FourierTransform (oracle/_ref), for pinning."""
+
+    def __init__(self, a, ecut, np0, np1, np2):
+        R = ref()
+        self.a = np.ascontiguousarray(a, dtype=np.float64).reshape(9)
+        self.hb = R.qbref_basis_create(_ptr(self.a), float(ecut), 1)
+        info = np.zeros(12, np.int32)
+        R.qbref_basis_info(self.hb, _ptr(info))
+        self.ngw = int(info[0])
+        self.n012 = np0 * np1 * np2
+        self.h = R.qbref_ft_create(self.hb, np0, np1, np2)
+
+    def __del__(self):
+        R = ref()
+        if getattr(self, "h", None):
+            R.qbref_ft_destroy(self.h)
+            R.qbref_basis_destroy(self.hb)
+            self.h = None
+
+    def backward(self, c):
+        c = np.ascontiguousarray(c, dtype=np.complex128)
+        f = np.zeros(self.n012, np.complex128)
+        ref().qbref_ft_backward(self.h, _ptr(c), _ptr(f))
+        return f
+
+    def forward(self, f):
+        f = np.array(f, dtype=np.complex128, copy=True)
+        c = np.zeros(self.ngw, np.complex128)
+        ref().qbref_ft_forward(self.h, _ptr(f), _ptr(c))
+        return c
+
+
+class Ham:
+    """Restated Hamiltonian (kinetic + local + KB nonlocal) and ETRS step."""
+
+    def __init__(self, ft, v_r, species):
+        """species: list of dicts {tau: (na,3), lmax, rc, wt: [w0,w1,w2]}."""
+        self.ft = ft
+        b = ft.basis
+        self.v_r = np.ascontiguousarray(v_r, dtype=np.float64)
+        nsp = len(species)
+        self.na = np.array([len(s["tau"]) for s in species], np.int32)
+        self.lmax = np.array([s["lmax"] for s in species], np.int32)
+        self.rc = np.array([s["rc"] for s in species], np.float64)
+        self.wt = np.zeros(3 * max(nsp, 1))
+        for i, s in enumerate(species):
+            w = list(s["wt"]) + [0.0] * 3
+            self.wt[3 * i:3 * i + 3] = w[:3]
+        self.tau = np.ascontiguousarray(
+            np.concatenate([np.asarray(s["tau"], np.float64).reshape(-1) for s in species])
+            if nsp else np.zeros(3), dtype=np.float64)
+        self.h = lib().qbo_ham_create(ft.h, b.ngw, _ptr(b.kpgx), b.omega, _ptr(self.v_r),
+                                      nsp, _ptr(self.na), _ptr(self.lmax), _ptr(self.rc),
+                                      _ptr(self.wt), _ptr(self.tau))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().qbo_ham_destroy(self.h)
+            self.h = None
+
+    def set_A(self, A):
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        lib().qbo_ham_set_A(self.h, _ptr(A))
+
+    def nproj(self):
+        return lib().qbo_ham_nproj(self.h)
+
+    def projector(self, p):
+        t = np.zeros(self.ft.basis.ngw)
+        l = ctypes.c_int()
+        w = ctypes.c_double()
+        tau = np.zeros(3)
+        lib().qbo_ham_projector(self.h, p, _ptr(t), ctypes.byref(l), ctypes.byref(w), _ptr(tau))
+        return t, l.value, w.value, tau
+
+    def hpsi(self, c, occ, nthreads=1):
+        c = np.asfortranarray(c, dtype=np.complex128)
+        ngw, nst = c.shape
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        cp = np.zeros_like(c, order="F")
+        enl = lib().qbo_hpsi(self.h, _ptr(c), ngw, nst, _ptr(occ), _ptr(cp), nthreads)
+        return cp, enl
+
+    def parts(self, c, occ, nthreads=1):
+        """(nonlocal, kinetic, local) contributions separately."""
+        c = np.asfortranarray(c, dtype=np.complex128)
+        ngw, nst = c.shape
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        out = []
+        cp = np.zeros_like(c, order="F")
+        enl = lib().qbo_nl_apply(self.h, _ptr(c), ngw, nst, _ptr(occ), _ptr(cp), nthreads)
+        out.append(cp)
+        cp = np.zeros_like(c, order="F")
+        lib().qbo_kinetic_add(self.h, _ptr(c), ngw, nst, _ptr(cp))
+        out.append(cp)
+        cp = np.zeros_like(c, order="F")
+        lib().qbo_rs_mul_add(self.h, _ptr(c), ngw, nst, _ptr(cp), nthreads)
+        out.append(cp)
+        return out, enl
+
+    def etrs_step(self, psi, occ, dt, A_t, A_tdt, want_rho=False, nthreads=1):
+        psi = np.asfortranarray(psi, dtype=np.complex128).copy(order="F")
+        ngw, nst = psi.shape
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        rho = np.zeros(self.ft.n012) if want_rho else None
+        A_t = np.ascontiguousarray(A_t, dtype=np.float64)
+        A_tdt = np.ascontiguousarray(A_tdt, dtype=np.float64)
+        nel = lib().qbo_etrs_step(self.h, _ptr(psi), ngw, nst, _ptr(occ), float(dt),
+                                  _ptr(A_t), _ptr(A_tdt), _ptr(rho), nthreads)
+        return psi, rho, nel
+
+
+def update_density(ft, c, occ, nthreads=1):
+    c = np.asfortranarray(c, dtype=np.complex128)
+    ngw, nst = c.shape
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    rho = np.zeros(ft.n012)
+    nel = lib().qbo_update_density(ft.h, _ptr(c), ngw, nst, _ptr(occ), ft.basis.omega,
+                                   _ptr(rho), nthreads)
+    return rho, nel
+
+
+def current_rs(ft, c, occ, A, nel):
+    c = np.asfortranarray(c, dtype=np.complex128)
+    ngw, nst = c.shape
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    J = np.zeros(3)
+    lib().qbo_current_rs(ft.h, _ptr(ft.basis.kpgx), ngw, _ptr(c), ngw, nst, _ptr(occ),
+                         ft.basis.omega, _ptr(A), float(nel), _ptr(J), 1)
+    return J
+
+
+def current_g(basis, c, occ, A, nel):
+    c = np.asfortranarray(c, dtype=np.complex128)
+    ngw, nst = c.shape
+    occ = np.ascontiguousarray(occ, dtype=np.float64)
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    J = np.zeros(3)
+    lib().qbo_current_g(_ptr(basis.kpgx), ngw, _ptr(c), ngw, nst, _ptr(occ), _ptr(A),
+                        float(nel), _ptr(J))
+    return J

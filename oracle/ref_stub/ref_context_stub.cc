@@ -1,0 +1,31 @@
+// One-process stand-in for the reference's BLACS/MPI Context and for the two
+// MPI queries made by its FourierTransform constructor.  It is test
+// infrastructure: it exists only so that the reference's own serial
+// Basis/FourierTransform/UnitCell sources can be compiled into oracle/_ref and
+// used as the pinned FFT oracle.  Every member answers as rank 0 of a 1x1 grid.
+#include <config.h>
+#include "Context.h"
+
+int MPI_Comm_size(int, int* size) { *size = 1; return 0; }
+int MPI_Comm_rank(int, int* rank) { *rank = 0; return 0; }
+
+Context::Context() : pimpl_(0) {}
+Context::~Context() {}
+int Context::ictxt() const { return 0; }
+int Context::myrow() const { return 0; }
+int Context::mycol() const { return 0; }
+int Context::nprow() const { return 1; }
+int Context::npcol() const { return 1; }
+int Context::size() const { return 1; }
+int Context::myproc() const { return 0; }
+int Context::mype() const { return 0; }
+bool Context::onpe0() const { return true; }
+bool Context::oncoutpe() const { return true; }
+int Context::coutpe() const { return 0; }
+bool Context::active() const { return true; }
+void Context::barrier() const {}
+MPI_Comm Context::comm() const { return 0; }
+void Context::isend(int, int, int*, int, int, int) const {}
+void Context::irecv(int, int, int*, int, int, int) const {}
+void Context::dsend(int, int, double*, int, int, int) const {}
+void Context::drecv(int, int, double*, int, int, int) const {}
