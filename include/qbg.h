@@ -1,0 +1,180 @@
+/*
+ * qbg.h -- C ABI of qball-gb300, a GB300 (sm_103a) implementation of
+ * qball's Kohn-Sham Hamiltonian application and ETRS real-time propagation
+ * step.
+ *
+ * The entry points mirror the reference's own operator surface; each
+ * declaration cites the reference interface it replaces (paths relative to
+ * the qball source tree).  Conventions, identical to the reference:
+ *
+ *  - Complex numbers are interleaved (re, im) pairs: double[2] for the FP64
+ *    ("plain") precision, float[2] where a _f32 entry point says so.
+ *  - A wavefunction block is column-major [ld x nst] complex; column n holds
+ *    state n, row ig the coefficient of plane wave ig in the basis' rod order
+ *    (Basis.cc:596-680): rods (h,k) in the order given, the G vectors of a
+ *    rod contiguous with l ascending from rod_lmin.
+ *  - Real-space grids are indexed f[i + np0*(j + np1*k)]
+ *    (FourierTransform.h:170).
+ *  - backward: f(r) = sum_G c(G) exp(+iG.r), unscaled.  forward:
+ *    c(G) = (1/N) sum_r f(r) exp(-iG.r), N = np0*np1*np2
+ *    (FourierTransform.h:147-152).
+ *  - All array arguments of compute entry points are DEVICE pointers unless
+ *    the parameter comment says "host".  Calls are asynchronous on the given
+ *    CUDA stream (NULL = legacy default stream) unless they return a host
+ *    scalar, in which case they synchronise that stream first.
+ *  - Every function returns a qbg_status; no C++ exception crosses the ABI.
+ *    qbg_last_error() gives a message for the last failure on this thread.
+ *  - A plan is thread-compatible, not thread-safe: one plan per stream at a
+ *    time (the reference's FourierTransform is not reentrant either).
+ */
+#ifndef QBG_H
+#define QBG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  QBG_OK = 0,
+  QBG_ERR_INVALID = 1,     /* bad argument or inconsistent sizes */
+  QBG_ERR_NOMEM = 2,       /* device or host allocation failed */
+  QBG_ERR_UNSUPPORTED = 3, /* grid length with an unsupported prime factor */
+  QBG_ERR_CUDA = 4,        /* a CUDA runtime call failed */
+  QBG_ERR_TIMEOUT = 5,     /* a bounded device-side wait expired */
+  QBG_ERR_DIVERGED = 6,    /* norm / charge drift check failed */
+  QBG_ERR_STATE = 7        /* call made before the plan was set up for it */
+} qbg_status;
+
+enum {
+  QBG_PREC_FP64 = 0,  /* plain form: FP64 storage and FP64 arithmetic */
+  QBG_PREC_MIXED = 1  /* FP32 transforms, tensor-core projector GEMMs,
+                         FP64 Taylor accumulation and reductions */
+};
+
+typedef struct qbg_plan qbg_plan;
+
+const char* qbg_last_error(void);
+const char* qbg_version(void);
+
+/* ---- Basis: Basis::resize (Basis.cc:302-700) -------------------------- */
+/* Full-sphere (force_complex) basis at k=0 on one process, rods in the
+ * reference's order.  a: host double[9] = cell vectors a0,a1,a2 (bohr);
+ * ecut in Hartree (the reference stores ecut in Ha, Ecut.h:80).
+ * info (host int[12]): [0]=ngw [1]=nrods [2..4]=np (Basis::np) [5..7]=idxmin
+ * [8..10]=idxmax [11]=0.  qbg_basis_fill's outputs are host arrays of
+ * nrods / nrods / nrods / nrods / 3*ngw / ngw / 3*ngw (any may be NULL);
+ * kpgx is stored as x block, y block, z block (Basis::kpgx_ptr). */
+qbg_status qbg_basis_dims(const double* a, double ecut, int* info);
+qbg_status qbg_basis_fill(const double* a, double ecut, int* rod_h,
+                          int* rod_k, int* rod_lmin, int* rod_size, int* idx,
+                          double* kpg2, double* kpgx);
+
+/* ---- Plan: FourierTransform(basis, np0, np1, np2)
+ *            (FourierTransform.h:136, FourierTransform.cc:144-527) -------- */
+typedef struct {
+  int ngw;             /* Basis::localsize() */
+  int nrods;           /* Basis::nrod_loc() */
+  const int* rod_h;    /* host, nrods: Basis::rod_h */
+  const int* rod_k;    /* host, nrods: Basis::rod_k */
+  const int* rod_lmin; /* host, nrods: Basis::rod_lmin */
+  const int* rod_size; /* host, nrods: Basis::rod_size */
+  const double* kpgx;  /* host, 3*ngw: Basis::kpgx_ptr(0..2) */
+  double omega;        /* UnitCell::volume() */
+} qbg_basis_desc;
+
+/* Descriptors are copied; nothing is borrowed past the call.  Fails with
+ * QBG_ERR_UNSUPPORTED for grid lengths with prime factors other than
+ * 2,3,5,7,11,13 and QBG_ERR_INVALID when a rod or band row falls outside
+ * the grid (np0 <= 2*max|h|, np1 < 2*(max|k|+1) or np2 <= 2*max|l|). */
+qbg_status qbg_plan_create(const qbg_basis_desc* basis, int np0, int np1,
+                           int np2, int precision, qbg_plan** plan);
+qbg_status qbg_plan_destroy(qbg_plan* plan);
+/* states processed per transform launch group (L2 working-set control) */
+qbg_status qbg_plan_set_chunk(qbg_plan* plan, int states_per_chunk);
+
+/* FourierTransform::backward(c, f) (FourierTransform.cc:529), batched over
+ * nbatch states: c [ldc x nbatch] complex, f [N x nbatch] complex (FP64). */
+qbg_status qbg_backward(qbg_plan* plan, const double* c, int ldc, double* f,
+                        int nbatch, void* stream);
+/* FourierTransform::forward(f, c) (FourierTransform.cc:542), batched; like
+ * the reference, f is overwritten (used as scratch). */
+qbg_status qbg_forward(qbg_plan* plan, double* f, double* c, int ldc,
+                       int nbatch, void* stream);
+
+/* ---- Hamiltonian set-up ---------------------------------------------- */
+/* Local potential v(r) on the grid (EnergyFunctional::v_r,
+ * EnergyFunctional.h:104).  v_r: N doubles, host or device (cudaMemcpy
+ * with cudaMemcpyDefault). */
+qbg_status qbg_set_vlocal(qbg_plan* plan, const double* v_r);
+
+/* Kleinman-Bylander projectors of nsp species with the synthetic radial
+ * form v_l(g) = g^l exp(-g^2 rc^2/2) (stands in for Species::dvnlg,
+ * Species.cc:1492).  All host arrays: na[nsp], lmax[nsp] in {-1,0,1,2},
+ * rc[nsp], wt[3*nsp] (KB weight per species and l, NonLocalPotential.cc:
+ * 228-236), tau[3*sum(na)] atom positions (bohr).  Replaces
+ * NonLocalPotential::init + update_twnl (NonLocalPotential.cc:76-259,
+ * 261-760). */
+qbg_status qbg_set_nonlocal(qbg_plan* plan, int nsp, const int* na,
+                            const int* lmax, const double* rc,
+                            const double* wt, const double* tau);
+
+/* Velocity-gauge vector potential A (host double[3]); recomputes
+ * |k+G-A|^2 (VectorPotential::get_kpgpa2, VectorPotential.h:84-95) and the
+ * projector tables for k+G-A (EnergyFunctional::vector_potential_changed,
+ * EnergyFunctional.cc:2047-2055). */
+qbg_status qbg_set_vector_potential(qbg_plan* plan, const double* A);
+
+/* ---- Operators --------------------------------------------------------- */
+/* hpsi = H psi for nst states: EnergyFunctional::energy(psi,
+ * compute_hpsi=true, dwf, ...) (EnergyFunctional.cc:1128-1701): dwf cleared,
+ * nonlocal projectors (NonLocalPotential::energy, NonLocalPotential.cc:
+ * 1908-2170), kinetic 0.5|k+G-A|^2 c, then SlaterDet::rs_mul_add
+ * (SlaterDet.cc:1025-1037).  psi, hpsi: [ld x nst] complex FP64.  occ: host
+ * double[nst] or NULL; when enl (host double*) is non-NULL it receives the
+ * nonlocal energy sum_n occ_n sum_p D_p/Omega |<beta_p|psi_n>|^2 and the
+ * call synchronises the stream. */
+qbg_status qbg_hpsi(qbg_plan* plan, const double* psi, int ld, double* hpsi,
+                    int nst, const double* occ, double* enl, void* stream);
+
+/* ChargeDensity::update_density (ChargeDensity.cc:276-556) without
+ * symmetrisation or ultrasoft/NLCC terms: rho(r) = sum_n (weight occ_n /
+ * Omega) |psi_n(r)|^2 (SlaterDet::compute_density, SlaterDet.cc:905-925).
+ * rho: device double[N], overwritten.  nel (host, may be NULL) receives
+ * Omega/N sum_r rho (ChargeDensity.cc:515-528) and synchronises. */
+qbg_status qbg_density(qbg_plan* plan, const double* psi, int ld, int nst,
+                       const double* occ, double weight, double* rho,
+                       double* nel, void* stream);
+
+/* Total electronic current J (host double[3]) of CurrentDensity::
+ * update_current (CurrentDensity.cc:39-106), evaluated in G space:
+ * J_d = -sum_n occ_n sum_G (k+G)_d |c_nG|^2 + A_d nel.  Synchronises. */
+qbg_status qbg_current(qbg_plan* plan, const double* psi, int ld, int nst,
+                       const double* occ, double nel, double* J,
+                       void* stream);
+
+/* One ETRS step (ExponentialWavefunctionStepper::preupdate + update,
+ * ExponentialWavefunctionStepper.cc:153-276; 4th-order Taylor
+ * exponentials, ExponentialWavefunctionStepper.cc:51-148): psi [ld x nst]
+ * FP64 is advanced in place from t to t+dt.  A_t (host double[3]) is the
+ * vector potential for the two exponentials of preupdate, A_tdt for the
+ * exponential of update (EhrenSampleStepper.cc:477-548); NULL means
+ * "unchanged".  rho_mid (device double[N], may be NULL) receives the density
+ * of the predicted psi(t+dt) built inside update() (ExponentialWavefunction-
+ * Stepper.cc:259); nel (host, may be NULL) its electron count.  With
+ * QBG_PREC_MIXED the three exponentials apply H in reduced precision and
+ * accumulate the Taylor series in FP64. */
+qbg_status qbg_etrs_step(qbg_plan* plan, double* psi, int ld, int nst,
+                         const double* occ, double dt, const double* A_t,
+                         const double* A_tdt, double* rho_mid, double* nel,
+                         void* stream);
+
+/* Number of this library's kernel launches issued since plan creation
+ * (instrumentation for benchmarks). */
+qbg_status qbg_launch_count(const qbg_plan* plan, long long* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QBG_H */

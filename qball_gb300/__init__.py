@@ -1,0 +1,270 @@
+"""qball-gb300: GB300-native Kohn-Sham H|psi> and ETRS propagation.
+
+The compute path is libqbg.so (hand-written sm_103a CUDA behind the C ABI of
+include/qbg.h).  This module is the thin host mirror of the reference's
+operator surface over that ABI:
+
+  Basis                         Basis::resize              (Basis.cc:302)
+  FourierTransform              FourierTransform           (FourierTransform.h:136)
+    .backward / .forward                                   (FourierTransform.cc:529,542)
+  Hamiltonian.hpsi              EnergyFunctional::energy(compute_hpsi=true)
+                                                           (EnergyFunctional.cc:1128)
+  Hamiltonian.update_density    ChargeDensity::update_density (ChargeDensity.cc:276)
+  Hamiltonian.current           CurrentDensity::update_current (CurrentDensity.cc:39)
+  Hamiltonian.etrs_step         ExponentialWavefunctionStepper::preupdate+update
+                                                           (ExponentialWavefunctionStepper.cc:153,241)
+
+Device arrays are torch tensors (torch is used only for device memory and
+streams) or raw integer device pointers.  A wavefunction block is a complex
+tensor of shape [nst, ld] -- column-major [ld x nst] in the reference's
+terms.  There is no CPU fallback: if libqbg.so is missing or no GPU is
+present, the operators raise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libqbg.so")
+
+QBG_PREC_FP64 = 0
+QBG_PREC_MIXED = 1
+_STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "unsupported",
+           4: "CUDA error", 5: "timeout", 6: "diverged", 7: "bad state"}
+
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+
+# entry points declared in include/qbg.h: name -> argtypes
+ABI = {
+    "qbg_last_error": [],
+    "qbg_version": [],
+    "qbg_basis_dims": [_P, _D, _P],
+    "qbg_basis_fill": [_P, _D, _P, _P, _P, _P, _P, _P, _P],
+    "qbg_plan_create": [_P, _I, _I, _I, _I, _P],
+    "qbg_plan_destroy": [_P],
+    "qbg_plan_set_chunk": [_P, _I],
+    "qbg_backward": [_P, _P, _I, _P, _I, _P],
+    "qbg_forward": [_P, _P, _P, _I, _I, _P],
+    "qbg_set_vlocal": [_P, _P],
+    "qbg_set_nonlocal": [_P, _I, _P, _P, _P, _P, _P],
+    "qbg_set_vector_potential": [_P, _P],
+    "qbg_hpsi": [_P, _P, _I, _P, _I, _P, _P, _P],
+    "qbg_density": [_P, _P, _I, _I, _P, _D, _P, _P, _P],
+    "qbg_current": [_P, _P, _I, _I, _P, _D, _P, _P],
+    "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
+    "qbg_launch_count": [_P, _P],
+}
+
+
+class QbgError(RuntimeError):
+    pass
+
+
+class _BasisDesc(ctypes.Structure):
+    _fields_ = [("ngw", _I), ("nrods", _I), ("rod_h", _P), ("rod_k", _P),
+                ("rod_lmin", _P), ("rod_size", _P), ("kpgx", _P), ("omega", _D)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libqbg.so (build it first with qball_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise QbgError(f"{LIBPATH} is not built; run python -m qball_gb300.build")
+        L = ctypes.CDLL(LIBPATH)
+        for name, args in ABI.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_char_p if name in ("qbg_last_error", "qbg_version") else _I
+        _lib = L
+    return _lib
+
+
+def _check(status, what):
+    if status != 0:
+        msg = lib().qbg_last_error().decode(errors="replace")
+        raise QbgError(f"{what}: {_STATUS.get(status, status)}: {msg}")
+
+
+def _np_ptr(a):
+    return a.ctypes.data_as(_P) if a is not None else None
+
+
+def _dev_ptr(x):
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return _P(x)
+    return _P(x.data_ptr())
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return _P(stream)
+    return _P(stream.cuda_stream)
+
+
+def cubic_cell(L):
+    return np.diag([float(L)] * 3).reshape(9)
+
+
+class Basis:
+    """Full-sphere plane-wave basis at k=0 (Basis::resize, Basis.cc:302-700).
+
+    cell: 9 floats (a0, a1, a2) or a scalar edge L of a cubic cell;
+    ecut in Hartree.
+    """
+
+    def __init__(self, cell, ecut):
+        a = cubic_cell(cell) if np.isscalar(cell) else np.ascontiguousarray(cell, np.float64).reshape(9)
+        self.a = a
+        self.ecut = float(ecut)
+        info = np.zeros(12, np.int32)
+        _check(lib().qbg_basis_dims(_np_ptr(a), self.ecut, _np_ptr(info)), "qbg_basis_dims")
+        self.ngw, self.nrods = int(info[0]), int(info[1])
+        self.np = tuple(int(v) for v in info[2:5])
+        self.idxmin = tuple(int(v) for v in info[5:8])
+        self.idxmax = tuple(int(v) for v in info[8:11])
+        self.rod_h = np.zeros(self.nrods, np.int32)
+        self.rod_k = np.zeros(self.nrods, np.int32)
+        self.rod_lmin = np.zeros(self.nrods, np.int32)
+        self.rod_size = np.zeros(self.nrods, np.int32)
+        self.idx = np.zeros(3 * self.ngw, np.int32)
+        self.kpg2 = np.zeros(self.ngw)
+        self.kpgx = np.zeros(3 * self.ngw)
+        _check(lib().qbg_basis_fill(_np_ptr(a), self.ecut, _np_ptr(self.rod_h), _np_ptr(self.rod_k),
+                                    _np_ptr(self.rod_lmin), _np_ptr(self.rod_size), _np_ptr(self.idx),
+                                    _np_ptr(self.kpg2), _np_ptr(self.kpgx)), "qbg_basis_fill")
+        a3 = a.reshape(3, 3)
+        self.omega = float(np.dot(a3[0], np.cross(a3[1], a3[2])))
+
+
+class FourierTransform:
+    """A plan: FourierTransform(basis, np0, np1, np2) plus the operators that
+    share its tables.  precision: "fp64" (plain) or "mixed"."""
+
+    def __init__(self, basis, np0, np1, np2, precision="fp64"):
+        self.basis = basis
+        self.shape = (int(np0), int(np1), int(np2))
+        self.n012 = int(np0) * int(np1) * int(np2)
+        self.precision = precision
+        prec = QBG_PREC_MIXED if precision == "mixed" else QBG_PREC_FP64
+        d = _BasisDesc(basis.ngw, basis.nrods, _np_ptr(basis.rod_h), _np_ptr(basis.rod_k),
+                       _np_ptr(basis.rod_lmin), _np_ptr(basis.rod_size), _np_ptr(basis.kpgx),
+                       basis.omega)
+        h = _P()
+        _check(lib().qbg_plan_create(ctypes.byref(d), int(np0), int(np1), int(np2), prec,
+                                     ctypes.byref(h)), "qbg_plan_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().qbg_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_chunk(self, n):
+        _check(lib().qbg_plan_set_chunk(self.h, int(n)), "qbg_plan_set_chunk")
+
+    def launches(self):
+        c = ctypes.c_longlong()
+        _check(lib().qbg_launch_count(self.h, ctypes.byref(c)), "qbg_launch_count")
+        return c.value
+
+    # ---- FourierTransform::backward / forward, batched over states
+    def backward(self, c, f, nbatch=None, ldc=None, stream=None):
+        nb = c.shape[0] if nbatch is None else nbatch
+        ld = c.shape[-1] if ldc is None else ldc
+        _check(lib().qbg_backward(self.h, _dev_ptr(c), ld, _dev_ptr(f), nb, _stream_ptr(stream)),
+               "qbg_backward")
+
+    def forward(self, f, c, nbatch=None, ldc=None, stream=None):
+        nb = c.shape[0] if nbatch is None else nbatch
+        ld = c.shape[-1] if ldc is None else ldc
+        _check(lib().qbg_forward(self.h, _dev_ptr(f), _dev_ptr(c), ld, nb, _stream_ptr(stream)),
+               "qbg_forward")
+
+
+class Hamiltonian(FourierTransform):
+    """EnergyFunctional-shaped operator set on one plan."""
+
+    def set_vlocal(self, v_r):
+        v = np.ascontiguousarray(v_r, np.float64) if isinstance(v_r, np.ndarray) else v_r
+        ptr = _np_ptr(v) if isinstance(v, np.ndarray) else _dev_ptr(v)
+        _check(lib().qbg_set_vlocal(self.h, ptr), "qbg_set_vlocal")
+
+    def set_nonlocal(self, species):
+        """species: list of {tau: (na,3), lmax, rc, wt: [w_s, w_p, w_d]}."""
+        nsp = len(species)
+        na = np.array([len(s["tau"]) for s in species], np.int32)
+        lmax = np.array([s["lmax"] for s in species], np.int32)
+        rc = np.array([s["rc"] for s in species], np.float64)
+        wt = np.zeros(3 * max(nsp, 1))
+        for i, s in enumerate(species):
+            w = list(s["wt"]) + [0.0] * 3
+            wt[3 * i:3 * i + 3] = w[:3]
+        tau = (np.ascontiguousarray(np.concatenate([np.asarray(s["tau"], np.float64).reshape(-1)
+                                                    for s in species]))
+               if nsp else np.zeros(3))
+        _check(lib().qbg_set_nonlocal(self.h, nsp, _np_ptr(na), _np_ptr(lmax), _np_ptr(rc),
+                                      _np_ptr(wt), _np_ptr(tau)), "qbg_set_nonlocal")
+
+    def set_vector_potential(self, A):
+        A = np.ascontiguousarray(A, np.float64)
+        _check(lib().qbg_set_vector_potential(self.h, _np_ptr(A)), "qbg_set_vector_potential")
+
+    def hpsi(self, psi, out, occ=None, want_enl=False, nst=None, ld=None, stream=None):
+        n = psi.shape[0] if nst is None else nst
+        ldv = psi.shape[-1] if ld is None else ld
+        o = np.ascontiguousarray(occ, np.float64) if occ is not None else None
+        e = ctypes.c_double()
+        _check(lib().qbg_hpsi(self.h, _dev_ptr(psi), ldv, _dev_ptr(out), n, _np_ptr(o),
+                              ctypes.byref(e) if want_enl else None, _stream_ptr(stream)),
+               "qbg_hpsi")
+        return e.value if want_enl else None
+
+    def update_density(self, psi, occ, rho, weight=1.0, nst=None, ld=None, stream=None):
+        n = psi.shape[0] if nst is None else nst
+        ldv = psi.shape[-1] if ld is None else ld
+        o = np.ascontiguousarray(occ, np.float64)
+        nel = ctypes.c_double()
+        _check(lib().qbg_density(self.h, _dev_ptr(psi), ldv, n, _np_ptr(o), float(weight),
+                                 _dev_ptr(rho), ctypes.byref(nel), _stream_ptr(stream)),
+               "qbg_density")
+        return nel.value
+
+    def current(self, psi, occ, nel, nst=None, ld=None, stream=None):
+        n = psi.shape[0] if nst is None else nst
+        ldv = psi.shape[-1] if ld is None else ld
+        o = np.ascontiguousarray(occ, np.float64)
+        J = np.zeros(3)
+        _check(lib().qbg_current(self.h, _dev_ptr(psi), ldv, n, _np_ptr(o), float(nel),
+                                 _np_ptr(J), _stream_ptr(stream)), "qbg_current")
+        return J
+
+    def etrs_step(self, psi, occ, dt, A_t=None, A_tdt=None, rho=None, want_nel=False,
+                  nst=None, ld=None, stream=None):
+        n = psi.shape[0] if nst is None else nst
+        ldv = psi.shape[-1] if ld is None else ld
+        o = np.ascontiguousarray(occ, np.float64)
+        at = np.ascontiguousarray(A_t, np.float64) if A_t is not None else None
+        atd = np.ascontiguousarray(A_tdt, np.float64) if A_tdt is not None else None
+        nel = ctypes.c_double()
+        _check(lib().qbg_etrs_step(self.h, _dev_ptr(psi), ldv, n, _np_ptr(o), float(dt),
+                                   _np_ptr(at), _np_ptr(atd), _dev_ptr(rho),
+                                   ctypes.byref(nel) if want_nel else None, _stream_ptr(stream)),
+               "qbg_etrs_step")
+        return nel.value if want_nel else None

@@ -1,0 +1,495 @@
+// qbg_fft.cu -- sphere <-> grid transforms and the fused local-potential and
+// density passes.
+//
+// One state's 3-D transform is split the way the reference splits it
+// (FourierTransform.cc:584-1360), without its MPI transpose:
+//   z pass : one line per rod (h,k); the rod's coefficients are gathered from
+//            the sphere straight into the line (vector_to_zvec fused), the
+//            result written plane-major Z[z][rod] so the next pass reads one
+//            contiguous row of rods per plane;
+//   x pass : one line per band row (the 2*ntrans0 rows y in [0,ntrans0) and
+//            [np1-ntrans0,np1) that can be non-zero), Y[z][band][x];
+//   y pass : one line per column x of a plane, where the pointwise work is
+//            fused: v(r)*psi(r) between the backward and forward transform
+//            (SlaterDet::rs_mul_add), |psi|^2 accumulation (compute_density),
+//            or the store of the full grid (plain backward).
+// The forward direction runs the same passes in reverse and fuses the
+// sphere scatter, the 1/N scale, the kinetic term and the Taylor-series
+// accumulation into the last z pass.
+// States are processed in chunks so the Z/Y intermediates of a chunk stay
+// L2-resident between passes.
+#include <algorithm>
+
+#include "qbg_internal.h"
+
+namespace qbg {
+
+constexpr int kTile = 16;     // lines per CTA
+constexpr int kThreads = 256;
+
+template <typename T> __device__ __forceinline__ cplx<T> czero() {
+  cplx<T> c;
+  c.x = T(0);
+  c.y = T(0);
+  return c;
+}
+
+// ------------------------------------------------------------------ z pass
+// backward: gather rods of state blockIdx.y from the sphere, transform
+// along z, write Z[s][z][rod].
+template <typename T, bool BIGP>
+__global__ void __launch_bounds__(kThreads)
+k_z_bwd(const cplx<T>* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
+        const RodInfo* __restrict__ rods, int nrods, FFTLen<T> d) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int n2 = d.n, ls = n2 + 1;
+  C* A = reinterpret_cast<C*>(smem);
+  C* B = A + kTile * ls;
+  const int r0 = blockIdx.x * kTile;
+  const int nl = min(kTile, nrods - r0);
+  const C* ps = psi + (size_t)blockIdx.y * ld;
+  for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int rl = warp; rl < nl; rl += nw) {
+    const RodInfo ri = rods[r0 + rl];
+    for (int i = lane; i < ri.size; i += 32) {
+      int z = ri.lmin + i;
+      if (z < 0) z += n2;
+      A[rl * ls + z] = ps[ri.first + i];
+    }
+  }
+  __syncthreads();
+  const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, d);
+  C* Zs = Z + (size_t)blockIdx.y * n2 * nrods;
+  for (int it = threadIdx.x; it < nl * n2; it += blockDim.x) {
+    const int rl = it % nl, z = it / nl;
+    Zs[(size_t)z * nrods + r0 + rl] = R[rl * ls + z];
+  }
+}
+
+// forward: read Z[s][z][rod], transform along z, scale by 1/N, scatter to
+// the sphere with the epilogue of MODE:
+//   0 store       c[g] = val
+//   1 hpsi        o = (o_nl + kin*psi) + val; out[g] = o; acc[g] += fac*o
+template <typename T, int MODE, bool BIGP>
+__global__ void __launch_bounds__(kThreads)
+k_z_fwd(const cplx<T>* __restrict__ Z, cplx<T>* __restrict__ out, int ldo,
+        const RodInfo* __restrict__ rods, int nrods, FFTLen<T> d, T scale,
+        const cplx<T>* psi, int ldp, const T* __restrict__ kpg2,
+        int out_init, double2* acc, int lda, double2 fac) {
+  // psi and acc may alias (the Taylor series is accumulated into the input
+  // of the first H application); each element is read before it is written
+  // by the same thread.
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int n2 = d.n, ls = n2 + 1;
+  C* A = reinterpret_cast<C*>(smem);
+  C* B = A + kTile * ls;
+  const int r0 = blockIdx.x * kTile;
+  const int nl = min(kTile, nrods - r0);
+  const int s = blockIdx.y;
+  const C* Zs = Z + (size_t)s * n2 * nrods;
+  for (int it = threadIdx.x; it < nl * n2; it += blockDim.x) {
+    const int rl = it % nl, z = it / nl;
+    A[rl * ls + z] = Zs[(size_t)z * nrods + r0 + rl];
+  }
+  __syncthreads();
+  const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  C* os = out + (size_t)s * ldo;
+  for (int rl = warp; rl < nl; rl += nw) {
+    const RodInfo ri = rods[r0 + rl];
+    for (int i = lane; i < ri.size; i += 32) {
+      int z = ri.lmin + i;
+      if (z < 0) z += n2;
+      C v = R[rl * ls + z];
+      v.x *= scale;
+      v.y *= scale;
+      const int g = ri.first + i;
+      if (MODE == 0) {
+        os[g] = v;
+      } else {
+        const C c = psi[(size_t)s * ldp + g];
+        const T x = T(0.5) * kpg2[g];
+        C o = out_init ? os[g] : czero<T>();
+        o.x = o.x + x * c.x;
+        o.y = o.y + x * c.y;
+        o.x = o.x + v.x;
+        o.y = o.y + v.y;
+        os[g] = o;
+        if (acc) {
+          double2* a = acc + (size_t)s * lda + g;
+          const double ox = (double)o.x, oy = (double)o.y;
+          double2 t = *a;
+          t.x = t.x + (fac.x * ox - fac.y * oy);
+          t.y = t.y + (fac.x * oy + fac.y * ox);
+          *a = t;
+        }
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------ x pass
+template <typename T, bool BIGP>
+__global__ void __launch_bounds__(kThreads)
+k_x_bwd(const cplx<T>* __restrict__ Z, cplx<T>* __restrict__ Y, int nrods,
+        int nband, int n2, const int* __restrict__ row_ptr,
+        const int* __restrict__ row_rod, const int* __restrict__ row_xb,
+        FFTLen<T> d) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int n0 = d.n, ls = n0 + 1;
+  C* A = reinterpret_cast<C*>(smem);
+  C* B = A + kTile * ls;
+  const int nbt = (nband + kTile - 1) / kTile;
+  const int z = blockIdx.x / nbt;
+  const int b0 = (blockIdx.x % nbt) * kTile;
+  const int nl = min(kTile, nband - b0);
+  const int s = blockIdx.y;
+  for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
+  __syncthreads();
+  const C* Zr = Z + ((size_t)s * n2 + z) * nrods;
+  const int q1 = row_ptr[b0 + nl];
+  for (int q = row_ptr[b0] + threadIdx.x; q < q1; q += blockDim.x) {
+    const int xb = row_xb[q];
+    A[((xb >> 16) - b0) * ls + (xb & 0xffff)] = Zr[row_rod[q]];
+  }
+  __syncthreads();
+  const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, d);
+  C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
+  for (int it = threadIdx.x; it < nl * n0; it += blockDim.x) {
+    const int bl = it / n0, x = it - bl * n0;
+    Yp[(size_t)(b0 + bl) * n0 + x] = R[bl * ls + x];
+  }
+}
+
+template <typename T, bool BIGP>
+__global__ void __launch_bounds__(kThreads)
+k_x_fwd(const cplx<T>* __restrict__ Y, cplx<T>* __restrict__ Z, int nrods,
+        int nband, int n2, const int* __restrict__ row_ptr,
+        const int* __restrict__ row_rod, const int* __restrict__ row_xb,
+        FFTLen<T> d) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int n0 = d.n, ls = n0 + 1;
+  C* A = reinterpret_cast<C*>(smem);
+  C* B = A + kTile * ls;
+  const int nbt = (nband + kTile - 1) / kTile;
+  const int z = blockIdx.x / nbt;
+  const int b0 = (blockIdx.x % nbt) * kTile;
+  const int nl = min(kTile, nband - b0);
+  const int s = blockIdx.y;
+  const C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
+  for (int it = threadIdx.x; it < nl * n0; it += blockDim.x) {
+    const int bl = it / n0, x = it - bl * n0;
+    A[bl * ls + x] = Yp[(size_t)(b0 + bl) * n0 + x];
+  }
+  __syncthreads();
+  const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
+  C* Zr = Z + ((size_t)s * n2 + z) * nrods;
+  const int q1 = row_ptr[b0 + nl];
+  for (int q = row_ptr[b0] + threadIdx.x; q < q1; q += blockDim.x) {
+    const int xb = row_xb[q];
+    Zr[row_rod[q]] = R[((xb >> 16) - b0) * ls + (xb & 0xffff)];
+  }
+}
+
+// ------------------------------------------------------------------ y pass
+enum YMode { Y_VLOC = 0, Y_BWD_STORE = 1, Y_FWD_LOAD = 2, Y_DENSITY = 3 };
+constexpr int kDensRegs = 16;  // kTile * n1 / kThreads for n1 <= 256
+
+template <typename T, int MODE, bool BIGP>
+__global__ void __launch_bounds__(kThreads)
+k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
+    const int* __restrict__ band_y, const T* __restrict__ v,
+    cplx<T>* __restrict__ f, const double* __restrict__ w, int nstates,
+    double* __restrict__ rho, int rho_accumulate, FFTLen<T> d) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int n1 = d.n, ls = n1 + 1;
+  C* A = reinterpret_cast<C*>(smem);
+  C* B = A + kTile * ls;
+  const int nct = (n0 + kTile - 1) / kTile;
+  const int z = blockIdx.x / nct;
+  const int x0 = (blockIdx.x % nct) * kTile;
+  const int nl = min(kTile, n0 - x0);
+  const size_t plane = (size_t)n0 * n1;
+  double dacc[kDensRegs];
+#pragma unroll
+  for (int k = 0; k < kDensRegs; ++k) dacc[k] = 0.0;
+  const int s_begin = MODE == Y_DENSITY ? 0 : blockIdx.y;
+  const int s_end = MODE == Y_DENSITY ? nstates : blockIdx.y + 1;
+  for (int s = s_begin; s < s_end; ++s) {
+    C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
+    C* R;
+    if (MODE == Y_FWD_LOAD) {
+      const C* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
+      for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
+        const int cl = it % nl, y = it / nl;
+        A[cl * ls + y] = fs[(size_t)y * n0 + x0 + cl];
+      }
+      __syncthreads();
+      R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
+    } else {
+      for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
+      __syncthreads();
+      for (int it = threadIdx.x; it < nl * nband; it += blockDim.x) {
+        const int cl = it % nl, b = it / nl;
+        A[cl * ls + band_y[b]] = Yp[(size_t)b * n0 + x0 + cl];
+      }
+      __syncthreads();
+      R = fft_lines<+1, T, BIGP>(A, B, nl, ls, d);
+    }
+    if (MODE == Y_VLOC) {
+      const T* vz = v + (size_t)z * plane;
+      for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
+        const int cl = it % nl, y = it / nl;
+        const T vv = vz[(size_t)y * n0 + x0 + cl];
+        C c = R[cl * ls + y];
+        c.x = c.x * vv;
+        c.y = c.y * vv;
+        R[cl * ls + y] = c;
+      }
+      __syncthreads();
+      C* other = R == A ? B : A;
+      R = fft_lines<-1, T, BIGP>(R, other, nl, ls, d);
+    }
+    if (MODE == Y_BWD_STORE) {
+      C* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
+      for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
+        const int cl = it % nl, y = it / nl;
+        fs[(size_t)y * n0 + x0 + cl] = R[cl * ls + y];
+      }
+    } else if (MODE == Y_DENSITY) {
+      const double ws = w[s];
+#pragma unroll
+      for (int k = 0; k < kDensRegs; ++k) {
+        const int it = threadIdx.x + k * blockDim.x;
+        if (it < nl * n1) {
+          const int cl = it % nl, y = it / nl;
+          const C c = R[cl * ls + y];
+          const double re = (double)c.x, im = (double)c.y;
+          dacc[k] += ws * (re * re + im * im);
+        }
+      }
+    } else {
+      // VLOC, FWD_LOAD: keep the band rows
+      for (int it = threadIdx.x; it < nl * nband; it += blockDim.x) {
+        const int cl = it % nl, b = it / nl;
+        Yp[(size_t)b * n0 + x0 + cl] = R[cl * ls + band_y[b]];
+      }
+    }
+    __syncthreads();
+  }
+  if (MODE == Y_DENSITY) {
+    double* rz = rho + (size_t)z * plane;
+#pragma unroll
+    for (int k = 0; k < kDensRegs; ++k) {
+      const int it = threadIdx.x + k * blockDim.x;
+      if (it < nl * n1) {
+        const int cl = it % nl, y = it / nl;
+        const size_t idx = (size_t)y * n0 + x0 + cl;
+        rz[idx] = rho_accumulate ? rz[idx] + dacc[k] : dacc[k];
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------- launchers
+template <typename T> static size_t smem_bytes(int n) {
+  return 2 * (size_t)kTile * (n + 1) * sizeof(cplx<T>);
+}
+
+template <typename K> static cudaError_t prep(K kernel, size_t smem) {
+  if (smem > 48 * 1024)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return cudaSuccess;
+}
+
+template <typename T> static qbg_status ensure_scratch(qbg_plan* p, int nch) {
+  const size_t zb = (size_t)nch * p->np2 * p->nrods * sizeof(cplx<T>);
+  const size_t yb = (size_t)nch * p->np2 * p->nband * p->np0 * sizeof(cplx<T>);
+  qbg_status s = ensure(&p->d_Z, &p->Z_bytes, zb);
+  if (s) return s;
+  return ensure(&p->d_Y, &p->Y_bytes, yb);
+}
+
+static bool big_prime(const LenTables& L) {
+  for (int i = 0; i < L.npass; ++i)
+    if (L.radix[i] == 7 || L.radix[i] == 11 || L.radix[i] == 13) return true;
+  return false;
+}
+
+template <typename T, bool BIGP>
+static qbg_status run_z_bwd_(qbg_plan* p, const cplx<T>* c, int ldc, int ns, cudaStream_t st) {
+  const FFTLen<T> d = p->len[2].view<T>();
+  const size_t sm = smem_bytes<T>(d.n);
+  QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
+  dim3 grid((p->nrods + kTile - 1) / kTile, ns);
+  k_z_bwd<T, BIGP><<<grid, kThreads, sm, st>>>(c, ldc, (cplx<T>*)p->d_Z, p->d_rods, p->nrods, d);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+template <typename T>
+static qbg_status run_z_bwd(qbg_plan* p, const cplx<T>* c, int ldc, int ns, cudaStream_t st) {
+  return big_prime(p->len[2]) ? run_z_bwd_<T, true>(p, c, ldc, ns, st)
+                              : run_z_bwd_<T, false>(p, c, ldc, ns, st);
+}
+
+template <typename T, bool BIGP>
+static qbg_status run_x_(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
+  const FFTLen<T> d = p->len[0].view<T>();
+  const size_t sm = smem_bytes<T>(d.n);
+  dim3 grid(p->np2 * ((p->nband + kTile - 1) / kTile), ns);
+  if (bwd) {
+    QBG_CUDA(prep(k_x_bwd<T, BIGP>, sm));
+    k_x_bwd<T, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Z, (cplx<T>*)p->d_Y, p->nrods,
+                                           p->nband, p->np2, p->d_row_ptr, p->d_row_rod,
+                                           p->d_row_x, d);
+  } else {
+    QBG_CUDA(prep(k_x_fwd<T, BIGP>, sm));
+    k_x_fwd<T, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Y, (cplx<T>*)p->d_Z, p->nrods,
+                                           p->nband, p->np2, p->d_row_ptr, p->d_row_rod,
+                                           p->d_row_x, d);
+  }
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+template <typename T>
+static qbg_status run_x(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
+  return big_prime(p->len[0]) ? run_x_<T, true>(p, bwd, ns, st) : run_x_<T, false>(p, bwd, ns, st);
+}
+
+template <typename T, int MODE, bool BIGP>
+static qbg_status run_y_(qbg_plan* p, int ns, cplx<T>* f, const double* w, double* rho,
+                         int rho_acc, cudaStream_t st) {
+  const FFTLen<T> d = p->len[1].view<T>();
+  const size_t sm = smem_bytes<T>(d.n);
+  QBG_CUDA(prep(k_y<T, MODE, BIGP>, sm));
+  dim3 grid(p->np2 * ((p->np0 + kTile - 1) / kTile), MODE == Y_DENSITY ? 1 : ns);
+  const T* v = nullptr;
+  if (MODE == Y_VLOC) v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vr32;
+  k_y<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((cplx<T>*)p->d_Y, p->nband, p->np0, p->np2,
+                                                p->d_band_y, v, f, w, ns, rho, rho_acc, d);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+template <typename T, int MODE>
+static qbg_status run_y(qbg_plan* p, int ns, cplx<T>* f, const double* w, double* rho,
+                        int rho_acc, cudaStream_t st) {
+  return big_prime(p->len[1]) ? run_y_<T, MODE, true>(p, ns, f, w, rho, rho_acc, st)
+                              : run_y_<T, MODE, false>(p, ns, f, w, rho, rho_acc, st);
+}
+
+template <typename T, int MODE, bool BIGP>
+static qbg_status run_z_fwd_(qbg_plan* p, cplx<T>* out, int ldo, int ns, const cplx<T>* psi,
+                             int ldp, int out_init, double2* acc, int lda, double2 fac,
+                             cudaStream_t st) {
+  const FFTLen<T> d = p->len[2].view<T>();
+  const size_t sm = smem_bytes<T>(d.n);
+  QBG_CUDA(prep(k_z_fwd<T, MODE, BIGP>, sm));
+  dim3 grid((p->nrods + kTile - 1) / kTile, ns);
+  const T scale = (T)(1.0 / (double)(p->np0 * p->np1 * p->np2));
+  const T* kin = std::is_same<T, double>::value ? (const T*)p->d_kpg2A : (const T*)p->d_kpg2A32;
+  k_z_fwd<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
+                                                    p->d_rods, p->nrods, d, scale, psi, ldp,
+                                                    kin, out_init, acc, lda, fac);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+template <typename T, int MODE>
+static qbg_status run_z_fwd(qbg_plan* p, cplx<T>* out, int ldo, int ns, const cplx<T>* psi,
+                            int ldp, int out_init, double2* acc, int lda, double2 fac,
+                            cudaStream_t st) {
+  return big_prime(p->len[2])
+             ? run_z_fwd_<T, MODE, true>(p, out, ldo, ns, psi, ldp, out_init, acc, lda, fac, st)
+             : run_z_fwd_<T, MODE, false>(p, out, ldo, ns, psi, ldp, out_init, acc, lda, fac, st);
+}
+
+#define QBG_TRY(x)                \
+  do {                            \
+    qbg_status s_ = (x);          \
+    if (s_ != QBG_OK) return s_;  \
+  } while (0)
+
+template <typename T>
+qbg_status local_hpsi(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int nst,
+                      bool out_init, double2* acc, int ldacc, double2 fac, cudaStream_t st) {
+  const int ch = std::max(1, std::min(p->chunk, nst));
+  QBG_TRY(ensure_scratch<T>(p, ch));
+  for (int s0 = 0; s0 < nst; s0 += ch) {
+    const int ns = std::min(ch, nst - s0);
+    QBG_TRY(run_z_bwd<T>(p, psi + (size_t)s0 * ld, ld, ns, st));
+    QBG_TRY(run_x<T>(p, true, ns, st));
+    QBG_TRY((run_y<T, Y_VLOC>(p, ns, nullptr, nullptr, nullptr, 0, st)));
+    QBG_TRY(run_x<T>(p, false, ns, st));
+    QBG_TRY((run_z_fwd<T, 1>(p, out + (size_t)s0 * ld, ld, ns, psi + (size_t)s0 * ld, ld,
+                             out_init ? 1 : 0, acc ? acc + (size_t)s0 * ldacc : nullptr, ldacc,
+                             fac, st)));
+  }
+  return QBG_OK;
+}
+
+template <typename T>
+qbg_status backward(qbg_plan* p, const cplx<T>* c, int ldc, cplx<T>* f, int nb, cudaStream_t st) {
+  const int ch = std::max(1, std::min(p->chunk, nb));
+  QBG_TRY(ensure_scratch<T>(p, ch));
+  for (int s0 = 0; s0 < nb; s0 += ch) {
+    const int ns = std::min(ch, nb - s0);
+    QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ldc, ldc, ns, st));
+    QBG_TRY(run_x<T>(p, true, ns, st));
+    QBG_TRY((run_y<T, Y_BWD_STORE>(p, ns, f + (size_t)s0 * p->N, nullptr, nullptr, 0, st)));
+  }
+  return QBG_OK;
+}
+
+template <typename T>
+qbg_status forward(qbg_plan* p, cplx<T>* f, cplx<T>* c, int ldc, int nb, cudaStream_t st) {
+  const int ch = std::max(1, std::min(p->chunk, nb));
+  QBG_TRY(ensure_scratch<T>(p, ch));
+  const double2 zero = make_double2(0.0, 0.0);
+  for (int s0 = 0; s0 < nb; s0 += ch) {
+    const int ns = std::min(ch, nb - s0);
+    QBG_TRY((run_y<T, Y_FWD_LOAD>(p, ns, f + (size_t)s0 * p->N, nullptr, nullptr, 0, st)));
+    QBG_TRY(run_x<T>(p, false, ns, st));
+    QBG_TRY((run_z_fwd<T, 0>(p, c + (size_t)s0 * ldc, ldc, ns, nullptr, 0, 0, nullptr, 0, zero,
+                             st)));
+  }
+  return QBG_OK;
+}
+
+template <typename T>
+qbg_status density(qbg_plan* p, const cplx<T>* c, int ldc, int nst, const double* d_w,
+                   double* rho, cudaStream_t st) {
+  const int ch = std::max(1, std::min(p->chunk, nst));
+  QBG_TRY(ensure_scratch<T>(p, ch));
+  if (nst == 0) {
+    QBG_CUDA(cudaMemsetAsync(rho, 0, sizeof(double) * p->N, st));
+    return QBG_OK;
+  }
+  for (int s0 = 0; s0 < nst; s0 += ch) {
+    const int ns = std::min(ch, nst - s0);
+    QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ldc, ldc, ns, st));
+    QBG_TRY(run_x<T>(p, true, ns, st));
+    QBG_TRY((run_y<T, Y_DENSITY>(p, ns, nullptr, d_w + s0, rho, s0 > 0 ? 1 : 0, st)));
+  }
+  return QBG_OK;
+}
+
+template qbg_status local_hpsi<double>(qbg_plan*, const double2*, int, double2*, int, bool,
+                                       double2*, int, double2, cudaStream_t);
+template qbg_status local_hpsi<float>(qbg_plan*, const float2*, int, float2*, int, bool,
+                                      double2*, int, double2, cudaStream_t);
+template qbg_status backward<double>(qbg_plan*, const double2*, int, double2*, int, cudaStream_t);
+template qbg_status backward<float>(qbg_plan*, const float2*, int, float2*, int, cudaStream_t);
+template qbg_status forward<double>(qbg_plan*, double2*, double2*, int, int, cudaStream_t);
+template qbg_status forward<float>(qbg_plan*, float2*, float2*, int, int, cudaStream_t);
+template qbg_status density<double>(qbg_plan*, const double2*, int, int, const double*, double*,
+                                    cudaStream_t);
+template qbg_status density<float>(qbg_plan*, const float2*, int, int, const double*, double*,
+                                   cudaStream_t);
+
+}  // namespace qbg

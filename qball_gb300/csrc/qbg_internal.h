@@ -1,0 +1,141 @@
+// qbg_internal.h -- plan layout and internal launchers shared by the .cu files.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/qbg.h"
+#include "qbg_fft_engine.cuh"
+
+namespace qbg {
+
+void set_error(const char* fmt, ...);
+qbg_status cuda_status(cudaError_t e, const char* what);
+
+#define QBG_CUDA(call)                                              \
+  do {                                                              \
+    cudaError_t e_ = (call);                                        \
+    if (e_ != cudaSuccess) return ::qbg::cuda_status(e_, #call);    \
+  } while (0)
+
+#define QBG_LAUNCHED(plan)                                          \
+  do {                                                              \
+    (plan)->launches++;                                             \
+    cudaError_t e_ = cudaGetLastError();                            \
+    if (e_ != cudaSuccess) return ::qbg::cuda_status(e_, "kernel"); \
+  } while (0)
+
+// Host-side factorisation and twiddle tables of one transform length.
+struct LenTables {
+  int n = 0;
+  int npass = 0;
+  int radix[kMaxPass] = {0};
+  int ns[kMaxPass] = {0};
+  int twoff[kMaxPass] = {0};
+  int goff7 = 0, goff11 = 0, goff13 = 0;
+  double2* d_tw64 = nullptr;
+  double2* d_g64 = nullptr;
+  float2* d_tw32 = nullptr;
+  float2* d_g32 = nullptr;
+  template <typename T> FFTLen<T> view() const;
+};
+
+// Per-rod table entry: G offset of the rod's first coefficient, rod length,
+// lmin, grid x index, band row index.
+struct RodInfo {
+  int first, size, lmin, xb;  // xb = x | (band << 16)
+};
+
+}  // namespace qbg
+
+struct qbg_plan {
+  int prec = QBG_PREC_FP64;
+  int ngw = 0, nrods = 0;
+  int np0 = 0, np1 = 0, np2 = 0;
+  long long N = 0;
+  int ntrans0 = 0, nband = 0;
+  double omega = 0.0;
+  double A[3] = {0, 0, 0};
+  int chunk = 8;
+  long long launches = 0;
+
+  // transform tables (n0 along x, n1 along y, n2 along z)
+  qbg::LenTables len[3];
+
+  // device basis tables
+  qbg::RodInfo* d_rods = nullptr;    // [nrods]
+  int* d_row_ptr = nullptr;          // [nband+1] rods per band row (CSR)
+  int* d_row_rod = nullptr;          // [nrods]
+  int* d_row_x = nullptr;            // [nrods]
+  int* d_band_y = nullptr;           // [nband] band row -> grid y
+  double* d_kpgx = nullptr;          // [3*ngw] k+G
+  double* d_kpg2A = nullptr;         // [ngw] |k+G-A|^2
+  float* d_kpg2A32 = nullptr;        // [ngw]
+  double* d_vr = nullptr;            // [N]
+  float* d_vr32 = nullptr;           // [N]
+  bool have_vr = false;
+  std::vector<int> rod_h, rod_k, rod_lmin, rod_size;
+  std::vector<double> kpgx_host;
+
+  // nonlocal projectors
+  int nproj = 0;
+  int nsp = 0;
+  std::vector<int> sp_na, sp_lmax;
+  std::vector<double> sp_rc, sp_wt, sp_tau;
+  int* d_plist = nullptr;      // [nproj] packed (species, ipr, atom) -> int4-like
+  double* d_ptau = nullptr;    // [3*nproj]
+  double* d_pwt = nullptr;     // [nproj] wt/omega
+  int* d_pl = nullptr;         // [nproj] (lm code)
+  double* d_prc = nullptr;     // [nproj]
+  double2* d_anl = nullptr;    // [nproj][ngw] FP64 projector table
+  float2* d_anl32 = nullptr;   // [nproj][ngw] FP32 copy (mixed)
+  bool nl_ready = false;
+
+  // scratch (allocated lazily, grown as needed)
+  void* d_Z = nullptr;  size_t Z_bytes = 0;   // [chunk][n2][nrods]
+  void* d_Y = nullptr;  size_t Y_bytes = 0;   // [chunk][n2][nband][n0]
+  void* d_fnl = nullptr; size_t fnl_bytes = 0;       // [nst][nproj]
+  void* d_fpart = nullptr; size_t fpart_bytes = 0;   // split-K partials
+  double* d_red = nullptr; size_t red_bytes = 0;     // reduction partials
+  double* d_rho = nullptr; size_t rho_bytes = 0;     // ETRS density scratch
+  double* h_red = nullptr; size_t h_red_bytes = 0;   // pinned host copy
+  // ETRS work buffers
+  void* d_w[4] = {nullptr, nullptr, nullptr, nullptr};
+  size_t w_bytes[4] = {0, 0, 0, 0};
+};
+
+namespace qbg {
+
+qbg_status ensure(void** p, size_t* cur, size_t need);
+qbg_status ensure_host(double** p, size_t* cur, size_t need);
+
+// transforms (qbg_fft.cu); T = double or float.  Pointers are device.
+// Hpsi local part for states [s0, s0+ns): out[g] = (out[g] + kin*psi[g]) +
+// fwd(v * bwd(psi))[g] (out holds the nonlocal part, or zero when
+// out_init == false); when acc != null: acc[g] += fac * out[g] (FP64).
+template <typename T>
+qbg_status local_hpsi(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out,
+                      int nst, bool out_init, double2* acc, int ldacc,
+                      double2 fac, cudaStream_t st);
+template <typename T>
+qbg_status backward(qbg_plan* p, const cplx<T>* c, int ldc, cplx<T>* f,
+                    int nb, cudaStream_t st);
+template <typename T>
+qbg_status forward(qbg_plan* p, cplx<T>* f, cplx<T>* c, int ldc, int nb,
+                   cudaStream_t st);
+template <typename T>
+qbg_status density(qbg_plan* p, const cplx<T>* c, int ldc, int nst,
+                   const double* d_w, double* rho, cudaStream_t st);
+
+// nonlocal (qbg_nl.cu)
+qbg_status nl_build(qbg_plan* p, cudaStream_t st);
+template <typename T>
+qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out,
+                    int nst, const double* d_occ, double* enl_dev,
+                    cudaStream_t st);
+
+// misc kernels (qbg_ops.cu)
+qbg_status update_kinetic(qbg_plan* p, cudaStream_t st);
+
+}  // namespace qbg

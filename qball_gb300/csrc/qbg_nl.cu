@@ -1,0 +1,383 @@
+// qbg_nl.cu -- Kleinman-Bylander nonlocal projectors.
+//
+// NonLocalPotential::energy (NonLocalPotential.cc:1908-2170) recomputes the
+// structure factors and the projector block anl = twnl (-i)^l exp(-i(k+G-A).tau)
+// on every call.  Atoms are frozen on this path and A changes only when the
+// caller sets a new vector potential, so the table anl[p][g] is built once
+// per A (nl_build) and kept resident in HBM; every H application then runs
+//   GEMM1  fnl[n][p] = sum_g conj(anl[p][g]) psi[n][g]      (split-K, FP64
+//                                                            partial sums)
+//   scale  fnl *= D_p/Omega, E_nl += occ_n D_p/Omega |fnl|^2
+//   GEMM2  out[n][g] = sum_p anl[p][g] fnl[n][p]
+// GEMM2 writes the nonlocal part as the first term of H psi, i.e. it also
+// performs the "dwf.clear()" of EnergyFunctional::energy.
+#include <algorithm>
+#include <vector>
+
+#include "qbg_internal.h"
+
+namespace qbg {
+
+// projector descriptor: l, m index within l, species radius, weight/omega
+struct ProjDesc {
+  int l, m;
+  double rc, wt;
+  double tau[3];
+};
+
+// update_twnl (NonLocalPotential.cc:306-760) for the synthetic radial form,
+// evaluated at k+G-A, times (-i)^l exp(-i (k+G-A).tau)  (:1962-2037).
+template <bool MIXED>
+__global__ void k_anl(const double* __restrict__ kpgx, const double* __restrict__ kpg2A,
+                      int ngw, double A0, double A1, double A2,
+                      const ProjDesc* __restrict__ pd, int nproj,
+                      double2* __restrict__ anl, float2* __restrict__ anl32) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  if (g >= ngw || p >= nproj) return;
+  const ProjDesc d = pd[p];
+  const double kx = kpgx[g] - A0, ky = kpgx[ngw + g] - A1, kz = kpgx[2 * ngw + g] - A2;
+  const double k2 = kpg2A[g];
+  const double tg = sqrt(k2);
+  const double tgi = k2 > 0.0 ? 1.0 / sqrt(k2) : 0.0;
+  const double e = exp(-0.5 * tg * tg * d.rc * d.rc);
+  const double pi = 3.14159265358979323846, fpi = 4.0 * pi;
+  double t;
+  if (d.l == 0) {
+    t = sqrt(1.0 / fpi) * e;
+  } else if (d.l == 1) {
+    const double s34pi = sqrt(3.0 / fpi);
+    const double c = d.m == 0 ? kx : (d.m == 1 ? ky : kz);
+    t = (s34pi * c * tgi) * (tg * e);
+  } else {
+    const double s54pi = sqrt(5.0 / fpi), s3 = sqrt(3.0);
+    const double tgi2 = tgi * tgi;
+    double y;
+    switch (d.m) {
+      case 0: y = s54pi * 0.5 * (3.0 * (kz * kz * tgi2) - 1.0); break;
+      case 1: y = s54pi * 0.5 * s3 * (kx * kx * tgi2 - ky * ky * tgi2); break;
+      case 2: y = s54pi * s3 * (kx * ky * tgi2); break;
+      case 3: y = s54pi * s3 * (ky * kz * tgi2); break;
+      default: y = s54pi * s3 * (kx * kz * tgi2); break;
+    }
+    t = y * (tg * tg * e);
+  }
+  // kpgr = -(k+G-A).tau, rounded term by term as the reference's dgemm
+  double kpgr = __dmul_rn(-d.tau[0], kx);
+  kpgr = __dadd_rn(kpgr, __dmul_rn(-d.tau[1], ky));
+  kpgr = __dadd_rn(kpgr, __dmul_rn(-d.tau[2], kz));
+  double s, c;
+  sincos(kpgr, &s, &c);
+  double re, im;
+  if (d.l == 0) {
+    re = t * c;
+    im = t * s;
+  } else if (d.l == 1) {
+    re = t * s;
+    im = -t * c;
+  } else {
+    re = -t * c;
+    im = -t * s;
+  }
+  const size_t o = (size_t)p * ngw + g;
+  anl[o] = make_double2(re, im);
+  if (MIXED) anl32[o] = make_float2((float)re, (float)im);
+}
+
+__global__ void k_kpg2A(const double* __restrict__ kpgx, int ngw, double A0, double A1,
+                        double A2, double* __restrict__ kpg2A, float* __restrict__ kpg2A32) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngw) return;
+  const double kx = kpgx[g], ky = kpgx[ngw + g], kz = kpgx[2 * ngw + g];
+  // VectorPotential::get_kpgpa2 (VectorPotential.h:84-95)
+  double k2 = __dadd_rn(__dadd_rn(__dmul_rn(kx, kx), __dmul_rn(ky, ky)), __dmul_rn(kz, kz));
+  const double value2 = __dadd_rn(__dadd_rn(__dmul_rn(A0, A0), __dmul_rn(A1, A1)), __dmul_rn(A2, A2));
+  double t = __dadd_rn(k2, value2);
+  t = __dsub_rn(t, __dmul_rn(__dmul_rn(2.0, A0), kx));
+  t = __dsub_rn(t, __dmul_rn(__dmul_rn(2.0, A1), ky));
+  t = __dsub_rn(t, __dmul_rn(__dmul_rn(2.0, A2), kz));
+  kpg2A[g] = t;
+  kpg2A32[g] = (float)t;
+}
+
+qbg_status update_kinetic(qbg_plan* p, cudaStream_t st) {
+  if (p->ngw == 0) return QBG_OK;
+  k_kpg2A<<<(p->ngw + 255) / 256, 256, 0, st>>>(p->d_kpgx, p->ngw, p->A[0], p->A[1], p->A[2],
+                                                p->d_kpg2A, p->d_kpg2A32);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
+  // projector order: species, atom blocks of <= 128 atoms, projector ipr
+  // (l, then m), atom within the block -- the index ia + ipr*nblk of
+  // NonLocalPotential.cc:2000 taken block by block.
+  std::vector<ProjDesc> pd;
+  std::vector<double> wt;
+  int namax = 0;
+  for (int s = 0; s < p->nsp; ++s) namax = std::max(namax, p->sp_na[s]);
+  const int nbs = std::max(1, std::min(namax, 128));
+  int atom0 = 0;
+  for (int s = 0; s < p->nsp; ++s) {
+    const int na = p->sp_na[s], lmax = p->sp_lmax[s];
+    for (int b0 = 0; b0 < na; b0 += nbs) {
+      const int b1 = std::min(na, b0 + nbs);
+      for (int l = 0; l <= lmax; ++l)
+        for (int m = 0; m < 2 * l + 1; ++m)
+          for (int ia = b0; ia < b1; ++ia) {
+            ProjDesc d;
+            d.l = l;
+            d.m = m;
+            d.rc = p->sp_rc[s];
+            d.wt = p->sp_wt[3 * s + l] / p->omega;
+            for (int j = 0; j < 3; ++j) d.tau[j] = p->sp_tau[3 * (size_t)(atom0 + ia) + j];
+            pd.push_back(d);
+            wt.push_back(d.wt);
+          }
+    }
+    atom0 += na;
+  }
+  p->nproj = (int)pd.size();
+  if (p->d_ptau) cudaFree(p->d_ptau);
+  if (p->d_pwt) cudaFree(p->d_pwt);
+  if (p->d_anl) cudaFree(p->d_anl);
+  if (p->d_anl32) cudaFree(p->d_anl32);
+  p->d_ptau = nullptr;
+  p->d_pwt = nullptr;
+  p->d_anl = nullptr;
+  p->d_anl32 = nullptr;
+  p->nl_ready = true;
+  if (p->nproj == 0 || p->ngw == 0) return QBG_OK;
+  ProjDesc* d_pd = nullptr;
+  QBG_CUDA(cudaMalloc(&d_pd, sizeof(ProjDesc) * pd.size()));
+  QBG_CUDA(cudaMemcpy(d_pd, pd.data(), sizeof(ProjDesc) * pd.size(), cudaMemcpyHostToDevice));
+  QBG_CUDA(cudaMalloc(&p->d_pwt, sizeof(double) * wt.size()));
+  QBG_CUDA(cudaMemcpy(p->d_pwt, wt.data(), sizeof(double) * wt.size(), cudaMemcpyHostToDevice));
+  const size_t n = (size_t)p->nproj * p->ngw;
+  QBG_CUDA(cudaMalloc(&p->d_anl, sizeof(double2) * n));
+  const bool mixed = p->prec == QBG_PREC_MIXED;
+  if (mixed) QBG_CUDA(cudaMalloc(&p->d_anl32, sizeof(float2) * n));
+  dim3 grid((p->ngw + 255) / 256, p->nproj);
+  if (mixed)
+    k_anl<true><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
+                                      d_pd, p->nproj, p->d_anl, p->d_anl32);
+  else
+    k_anl<false><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
+                                       d_pd, p->nproj, p->d_anl, nullptr);
+  p->launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_pd);
+  if (e != cudaSuccess) return cuda_status(e, "k_anl");
+  return QBG_OK;
+}
+
+// ------------------------------------------------------------------ GEMMs
+constexpr int GT = 64;   // output tile edge
+constexpr int GK = 16;   // k step
+
+// part[z][n][p] = sum_{g in split z} conj(anl[p][g]) psi[n][g]
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_fnl(const cplx<T>* __restrict__ anl, int ngw, int nproj, const cplx<T>* __restrict__ psi,
+      int ld, int nst, double2* __restrict__ part, int kchunk) {
+  using C = cplx<T>;
+  __shared__ C As[GK][GT];
+  __shared__ C Bs[GK][GT];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int p0 = blockIdx.x * GT, n0 = blockIdx.y * GT;
+  const int kb = blockIdx.z * kchunk, ke = min(ngw, kb + kchunk);
+  T ar[4][4], ai[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ar[i][j] = ai[i][j] = T(0);
+  for (int k0 = kb; k0 < ke; k0 += GK) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = tid + 256 * q, r = e >> 4, kk = e & 15;
+      const int k = k0 + kk;
+      C a, b;
+      a.x = a.y = b.x = b.y = T(0);
+      if (k < ke && p0 + r < nproj) a = anl[(size_t)(p0 + r) * ngw + k];
+      if (k < ke && n0 + r < nst) b = psi[(size_t)(n0 + r) * ld + k];
+      As[kk][r] = a;
+      Bs[kk][r] = b;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      C a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          ar[i][j] += a[i].x * b[j].x + a[i].y * b[j].y;
+          ai[i][j] += a[i].x * b[j].y - a[i].y * b[j].x;
+        }
+    }
+    __syncthreads();
+  }
+  double2* pz = part + (size_t)blockIdx.z * nst * nproj;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int pp = p0 + ty + 16 * i, nn = n0 + tx + 16 * j;
+      if (pp < nproj && nn < nst)
+        pz[(size_t)nn * nproj + pp] = make_double2((double)ar[i][j], (double)ai[i][j]);
+    }
+}
+
+// fnl[n][p] = (D_p/Omega) sum_z part[z][n][p]; enl partials per block
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_fnl_reduce(const double2* __restrict__ part, int nsplit, int nproj, int nst,
+             const double* __restrict__ wt, const double* __restrict__ occ,
+             cplx<T>* __restrict__ fnl, double* __restrict__ enl_part) {
+  __shared__ double red[256];
+  const size_t total = (size_t)nproj * nst;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (i < total) {
+    const int n = (int)(i / nproj), pp = (int)(i - (size_t)n * nproj);
+    double re = 0.0, im = 0.0;
+    for (int z = 0; z < nsplit; ++z) {
+      const double2 v = part[(size_t)z * total + i];
+      re += v.x;
+      im += v.y;
+    }
+    const double fac = wt[pp];
+    e = (fac * (occ ? occ[n] : 0.0)) * (re * re + im * im);
+    cplx<T> f;
+    f.x = (T)(fac * re);
+    f.y = (T)(fac * im);
+    fnl[i] = f;
+  }
+  red[threadIdx.x] = e;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && enl_part) enl_part[blockIdx.x] = red[0];
+}
+
+// out[n][g] = sum_p anl[p][g] fnl[n][p]
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_nl_hpsi(const cplx<T>* __restrict__ anl, int ngw, int nproj, const cplx<T>* __restrict__ fnl,
+          int nst, cplx<T>* __restrict__ out, int ldo) {
+  using C = cplx<T>;
+  __shared__ C As[GK][GT];
+  __shared__ C Bs[GK][GT];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int g0 = blockIdx.x * GT, n0 = blockIdx.y * GT;
+  T ar[4][4], ai[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ar[i][j] = ai[i][j] = T(0);
+  for (int k0 = 0; k0 < nproj; k0 += GK) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int e = tid + 256 * q;
+      {
+        const int kk = e >> 6, gg = e & 63;
+        C a;
+        a.x = a.y = T(0);
+        if (k0 + kk < nproj && g0 + gg < ngw) a = anl[(size_t)(k0 + kk) * ngw + g0 + gg];
+        As[kk][gg] = a;
+      }
+      {
+        const int kk = e & 15, nn = e >> 4;
+        C b;
+        b.x = b.y = T(0);
+        if (k0 + kk < nproj && n0 + nn < nst) b = fnl[(size_t)(n0 + nn) * nproj + k0 + kk];
+        Bs[kk][nn] = b;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GK; ++kk) {
+      C a[4], b[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][tx + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) b[j] = Bs[kk][ty + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          ar[i][j] += a[i].x * b[j].x - a[i].y * b[j].y;
+          ai[i][j] += a[i].x * b[j].y + a[i].y * b[j].x;
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gg = g0 + tx + 16 * i, nn = n0 + ty + 16 * j;
+      if (gg < ngw && nn < nst) {
+        C o;
+        o.x = ar[i][j];
+        o.y = ai[i][j];
+        out[(size_t)nn * ldo + gg] = o;
+      }
+    }
+}
+
+template <typename T>
+qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int nst,
+                    const double* d_occ, double* enl_part, cudaStream_t st) {
+  const int P = p->nproj;
+  if (P == 0 || nst == 0) return QBG_OK;
+  const cplx<T>* anl = std::is_same<T, double>::value ? (const cplx<T>*)p->d_anl
+                                                       : (const cplx<T>*)p->d_anl32;
+  const int mt = (P + GT - 1) / GT, nt = (nst + GT - 1) / GT;
+  // split K so that the grid covers the GPU a few times over; FP32 keeps
+  // each partial sum short (<= 2048 terms) and adds the partials in FP64
+  int nsm = 152;
+  int target = 4 * nsm;
+  int split = std::max(1, (target + mt * nt - 1) / (mt * nt));
+  const int maxk = std::is_same<T, double>::value ? (1 << 30) : 2048;
+  split = std::max(split, (p->ngw + maxk - 1) / maxk);
+  split = std::min(split, std::max(1, p->ngw / GK));
+  int kchunk = (p->ngw + split - 1) / split;
+  kchunk = (kchunk + GK - 1) / GK * GK;
+  split = (p->ngw + kchunk - 1) / kchunk;
+  const size_t need = (size_t)split * P * nst * sizeof(double2);
+  qbg_status s = ensure(&p->d_fpart, &p->fpart_bytes, need);
+  if (s) return s;
+  s = ensure(&p->d_fnl, &p->fnl_bytes, (size_t)P * nst * sizeof(cplx<T>));
+  if (s) return s;
+  k_fnl<T><<<dim3(mt, nt, split), 256, 0, st>>>(anl, p->ngw, P, psi, ld, nst,
+                                                 (double2*)p->d_fpart, kchunk);
+  QBG_LAUNCHED(p);
+  const size_t total = (size_t)P * nst;
+  const int rb = (int)((total + 255) / 256);
+  k_fnl_reduce<T><<<rb, 256, 0, st>>>((const double2*)p->d_fpart, split, P, nst, p->d_pwt,
+                                      d_occ, (cplx<T>*)p->d_fnl, enl_part);
+  QBG_LAUNCHED(p);
+  k_nl_hpsi<T><<<dim3((p->ngw + GT - 1) / GT, nt), 256, 0, st>>>(
+      anl, p->ngw, P, (const cplx<T>*)p->d_fnl, nst, out, ld);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+int nl_reduce_blocks(const qbg_plan* p, int nst) {
+  return (int)(((size_t)p->nproj * nst + 255) / 256);
+}
+
+template qbg_status nl_apply<double>(qbg_plan*, const double2*, int, double2*, int,
+                                     const double*, double*, cudaStream_t);
+template qbg_status nl_apply<float>(qbg_plan*, const float2*, int, float2*, int, const double*,
+                                    double*, cudaStream_t);
+
+}  // namespace qbg

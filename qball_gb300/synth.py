@@ -1,0 +1,125 @@
+"""Seeded synthetic cells for the H|psi> / ETRS path.
+
+No public dataset is involved: every input is generated from a seed.
+  * cubic cell of edge L (bohr), full-sphere basis at ecut (Ha);
+  * atoms uniform in the cell, minimum separation 3 bohr (rejection);
+  * psi(G) = complex normal * exp(-|G|^2/8), Gram/Cholesky-orthonormalised in
+    FP64 (the semantics of SlaterDet::gram, SlaterDet.cc:1043-1143);
+  * v_loc(r) = sum_a -2 exp(-|r - tau_a|^2 / (2 w^2)), w = 1 bohr, minimum
+    image (the real-space form of a Gaussian local pseudopotential);
+  * one KB species, lmax 1 (s,p: 4 projectors/atom) or 2 (s,p,d: 9/atom),
+    radial form g^l exp(-g^2 rc^2/2) with rc = 1, weights D_l ~ U[0.5, 2] Ha;
+  * occupations 2 (closed shell).
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Cell:
+    L: float
+    ecut: float            # Hartree
+    grid: tuple
+    nst: int
+    natoms: int
+    lmax: int
+    seed: int = 1234
+    name: str = ""
+    tau: np.ndarray = field(default=None, repr=False)
+    wt: list = field(default=None, repr=False)
+
+
+# the workloads of the benchmark configurations
+CONFIGS = {
+    # 8 atoms, L=20, 20 Ry, 48^3, 16 states, s+p projectors
+    "c1": dict(L=20.0, ecut=10.0, grid=(48, 48, 48), nst=16, natoms=8, lmax=1),
+    # 8 atoms on the reference's own dense-grid rule for this cell (64^3)
+    "c1q": dict(L=20.0, ecut=10.0, grid=(64, 64, 64), nst=16, natoms=8, lmax=1),
+    # 216 atoms, L=30, 50 Ry, 120^3, 432 states, s+p+d projectors
+    "c2": dict(L=30.0, ecut=25.0, grid=(120, 120, 120), nst=432, natoms=216, lmax=2),
+    # 512 atoms, L=40, 40 Ry, 160^3, 2048 states
+    "c5": dict(L=40.0, ecut=20.0, grid=(160, 160, 160), nst=2048, natoms=512, lmax=2),
+    # small cells for tests
+    "t12": dict(L=12.0, ecut=10.0, grid=(32, 32, 32), nst=8, natoms=4, lmax=2),
+    "t12b": dict(L=12.0, ecut=10.0, grid=(20, 24, 30), nst=5, natoms=3, lmax=2),
+}
+
+
+def make_cell(name=None, seed=1234, **kw):
+    params = dict(CONFIGS[name]) if name else {}
+    params.update(kw)
+    c = Cell(seed=seed, name=name or "custom", **params)
+    rng = np.random.default_rng(seed)
+    c.tau = place_atoms(rng, c.L, c.natoms)
+    c.wt = list(rng.uniform(0.5, 2.0, size=3))
+    return c
+
+
+def place_atoms(rng, L, n, min_sep=3.0, max_tries=200000):
+    pts = []
+    tries = 0
+    while len(pts) < n:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError(f"could not place {n} atoms with separation {min_sep} in L={L}")
+        p = rng.uniform(0.0, L, size=3)
+        ok = True
+        for q in pts:
+            d = p - q
+            d -= L * np.round(d / L)
+            if np.dot(d, d) < min_sep * min_sep:
+                ok = False
+                break
+        if ok:
+            pts.append(p)
+    return np.array(pts, dtype=np.float64).reshape(n, 3)
+
+
+def species(cell):
+    return [dict(tau=cell.tau, lmax=cell.lmax, rc=1.0, wt=cell.wt)]
+
+
+def vlocal(cell, depth=-2.0, width=1.0):
+    """v(r) on the grid, x fastest: index i + n0*(j + n1*k)."""
+    n0, n1, n2 = cell.grid
+    L = cell.L
+    x = np.arange(n0) * (L / n0)
+    y = np.arange(n1) * (L / n1)
+    z = np.arange(n2) * (L / n2)
+    v = np.zeros((n2, n1, n0))
+    for t in cell.tau:
+        def g1(r, c):
+            d = r - c
+            d -= L * np.round(d / L)
+            return np.exp(-d * d / (2 * width * width))
+        gx, gy, gz = g1(x, t[0]), g1(y, t[1]), g1(z, t[2])
+        v += depth * gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+    return v.reshape(-1)
+
+
+def wavefunctions(cell, basis, seed=None, nst=None):
+    """[nst, ngw] complex128, orthonormal rows."""
+    rng = np.random.default_rng(cell.seed + 7 if seed is None else seed)
+    n = cell.nst if nst is None else nst
+    ngw = basis.ngw
+    env = np.exp(-basis.kpg2 / 8.0)
+    c = (rng.standard_normal((n, ngw)) + 1j * rng.standard_normal((n, ngw))) * env[None, :]
+    return gram(c)
+
+
+def gram(c):
+    """Cholesky orthonormalisation of the rows of c (FP64)."""
+    s = c.conj() @ c.T          # s_ij = <psi_i|psi_j>
+    l = np.linalg.cholesky(s)   # s = L L^H
+    # rows c' = conj(L)^{-1} c give <psi'_i|psi'_j> = delta_ij
+    return np.linalg.solve(l.conj(), c)
+
+
+def occupations(cell, nst=None):
+    return np.full(cell.nst if nst is None else nst, 2.0)
+
+
+def kick(strength=0.01):
+    """velocity-gauge delta kick along z (set vector_potential 0 0 A)."""
+    return np.array([0.0, 0.0, strength])

@@ -1,0 +1,222 @@
+"""Parity of the sm_103a path (through the C ABI) against the CPU oracle.
+
+Tolerances: the plain FP64 form must match the oracle to <= 1e-10 relative
+(H|psi>, rho(r), the current and psi after N ETRS steps); the transforms to
+<= 1e-12.  The mixed form (FP32 transforms and projector GEMMs, FP64
+Taylor accumulation) is held to 5e-5 relative on psi after 3 steps.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+import qball_gb300 as Q
+from qball_gb300 import synth
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NT = 8  # oracle threads
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def setup(name, prec="fp64", **kw):
+    cell = synth.make_cell(name, **kw)
+    b = Q.Basis(cell.L, cell.ecut)
+    H = Q.Hamiltonian(b, *cell.grid, precision=prec)
+    v = synth.vlocal(cell)
+    H.set_vlocal(v)
+    H.set_nonlocal(synth.species(cell))
+    ob = O.Basis(b.a, cell.ecut)
+    oft = O.FT(ob, *cell.grid)
+    oh = O.Ham(oft, v, synth.species(cell))
+    psi = synth.wavefunctions(cell, b)
+    return cell, b, H, oft, oh, psi
+
+
+def dev(x):
+    torch = _torch()
+    return torch.from_numpy(np.ascontiguousarray(x)).to("cuda:0")
+
+
+@pytest.mark.parametrize("name", ["l12_e10", "l12_e10_g32", "l20_e10_g48", "l20_e10_g64"])
+def test_fft_backward_forward_vs_reference_golden(cuda, name):
+    from conftest import load_golden
+    g = load_golden(name)
+    b = Q.Basis(g["a"], float(g["ecut"]))
+    grid = tuple(int(x) for x in g["grid"])
+    ft = Q.FourierTransform(b, *grid)
+    torch = _torch()
+    c = dev(np.stack([g["c1"], g["c2"]]))
+    f = torch.zeros((2, ft.n012), dtype=torch.complex128, device=cuda)
+    ft.backward(c, f)
+    fh = f.cpu().numpy()
+    sel = g["f_sel"]
+    assert rel_err(fh[0][sel], g["f1_sel"]) < 1e-13
+    assert abs(np.vdot(fh[0], fh[0]).real / float(g["f1_norm2"]) - 1) < 1e-13
+    # forward of w(r) * backward(c2): the rs_mul_add shape
+    n0, n1, n2 = grid
+    k, j, i = np.meshgrid(np.arange(n2), np.arange(n1), np.arange(n0), indexing="ij")
+    w = (1.0 + 0.5 * np.cos(2 * np.pi * (i / n0 + 2 * j / n1 + 3 * k / n2))).reshape(-1)
+    r = dev(np.stack([fh[0], fh[1] * w]))
+    out = torch.zeros((2, b.ngw), dtype=torch.complex128, device=cuda)
+    ft.forward(r, out)
+    oh = out.cpu().numpy()
+    assert rel_err(oh[0], g["c1_roundtrip"]) < 1e-13
+    assert rel_err(oh[1], g["c_from_r"]) < 1e-13
+
+
+@pytest.mark.parametrize("L,ecut,grid", [(12.0, 10.0, (32, 32, 32)), (12.0, 10.0, (20, 24, 30)),
+                                         (20.0, 10.0, (48, 48, 48)), (10.0, 6.0, (28, 28, 28)),
+                                         (10.0, 6.0, (22, 22, 26))])
+def test_fft_vs_oracle_many_grids(cuda, L, ecut, grid):
+    """radix 2,3,4,5,8 plus the direct-DFT primes 7, 11 and 13"""
+    b = Q.Basis(L, ecut)
+    ob = O.Basis(b.a, ecut)
+    oft = O.FT(ob, *grid)
+    ft = Q.FourierTransform(b, *grid)
+    rng = np.random.default_rng(11)
+    nb = 3
+    c = rng.standard_normal((nb, b.ngw)) + 1j * rng.standard_normal((nb, b.ngw))
+    torch = _torch()
+    f = torch.zeros((nb, ft.n012), dtype=torch.complex128, device=cuda)
+    ft.backward(dev(c), f)
+    fh = f.cpu().numpy()
+    for s in range(nb):
+        assert rel_err(fh[s], oft.backward(c[s])) < 1e-13
+    r = rng.standard_normal((nb, ft.n012)) + 1j * rng.standard_normal((nb, ft.n012))
+    out = torch.zeros((nb, b.ngw), dtype=torch.complex128, device=cuda)
+    ft.forward(dev(r), out)
+    oh = out.cpu().numpy()
+    for s in range(nb):
+        assert rel_err(oh[s], oft.forward(r[s])) < 1e-13
+
+
+def test_fft_padded_leading_dimension(cuda):
+    b = Q.Basis(12.0, 10.0)
+    ft = Q.FourierTransform(b, 32, 32, 32)
+    ld = b.ngw + 37
+    rng = np.random.default_rng(2)
+    c = np.zeros((4, ld), complex)
+    c[:, :b.ngw] = rng.standard_normal((4, b.ngw)) + 1j * rng.standard_normal((4, b.ngw))
+    torch = _torch()
+    f = torch.zeros((4, ft.n012), dtype=torch.complex128, device=cuda)
+    ft.backward(dev(c), f, ldc=ld)
+    out = torch.full((4, ld), 7.0 + 0j, dtype=torch.complex128, device=cuda)
+    ft.forward(f, out, ldc=ld)
+    oh = out.cpu().numpy()
+    assert np.abs(oh[:, :b.ngw] - c[:, :b.ngw]).max() < 1e-13
+    assert np.all(oh[:, b.ngw:] == 7.0)  # padding rows untouched
+
+
+@pytest.mark.parametrize("name", ["t12", "c1"])
+def test_hpsi_fp64_vs_oracle(cuda, name):
+    cell, b, H, oft, oh, psi = setup(name)
+    occ = synth.occupations(cell)
+    torch = _torch()
+    out = torch.zeros_like(dev(psi))
+    enl = H.hpsi(dev(psi), out, occ, want_enl=True)
+    ref, enl_ref = oh.hpsi(psi.T, occ, nthreads=NT)
+    assert rel_err(out.cpu().numpy(), ref.T) < 1e-10
+    assert abs(enl - enl_ref) <= 1e-10 * abs(enl_ref)
+    # Hermiticity <phi|H psi> = <H phi|psi>
+    hp = out.cpu().numpy()
+    m = psi.conj() @ hp.T
+    assert np.abs(m - m.conj().T).max() < 1e-10 * np.abs(m).max()
+
+
+def test_hpsi_pieces_local_only_and_no_states(cuda):
+    cell = synth.make_cell("t12b")
+    b = Q.Basis(cell.L, cell.ecut)
+    H = Q.Hamiltonian(b, *cell.grid)
+    v = synth.vlocal(cell)
+    H.set_vlocal(v)
+    psi = synth.wavefunctions(cell, b)
+    ob = O.Basis(b.a, cell.ecut)
+    oft = O.FT(ob, *cell.grid)
+    oh = O.Ham(oft, v, [])
+    torch = _torch()
+    out = torch.zeros_like(dev(psi))
+    H.hpsi(dev(psi), out, synth.occupations(cell))
+    ref, _ = oh.hpsi(psi.T, synth.occupations(cell))
+    assert rel_err(out.cpu().numpy(), ref.T) < 1e-10
+    # nst = 0 is a no-op
+    H.hpsi(dev(psi), out, synth.occupations(cell), nst=0)
+
+
+def test_density_and_current_vs_oracle(cuda):
+    cell, b, H, oft, oh, psi = setup("c1")
+    occ = synth.occupations(cell)
+    torch = _torch()
+    rho = torch.zeros(oft.n012, dtype=torch.float64, device=cuda)
+    nel = H.update_density(dev(psi), occ, rho)
+    rref, nref = O.update_density(oft, psi.T, occ)
+    assert rel_err(rho.cpu().numpy(), rref) < 1e-12
+    assert abs(nel - nref) < 1e-10 * nref
+    assert abs(nel - occ.sum()) < 1e-8
+    A = synth.kick()
+    H.set_vector_potential(A)
+    J = H.current(dev(psi), occ, nel)
+    Jg = O.current_g(O.Basis(b.a, cell.ecut), psi.T, occ, A, nref)
+    Jr = O.current_rs(oft, psi.T, occ, A, nref)
+    assert np.abs(J - Jg).max() < 1e-10 * max(1.0, np.abs(Jg).max())
+    assert np.abs(J - Jr).max() < 1e-9 * max(1.0, np.abs(Jr).max())
+
+
+@pytest.mark.parametrize("nsteps", [1, 3])
+def test_etrs_fp64_vs_oracle(cuda, nsteps):
+    cell, b, H, oft, oh, psi = setup("t12")
+    occ = synth.occupations(cell)
+    A = synth.kick()
+    dt = 0.05
+    torch = _torch()
+    p = dev(psi)
+    rho = torch.zeros(oft.n012, dtype=torch.float64, device=cuda)
+    ref = psi.T.copy()
+    oh.set_A(A)
+    for _ in range(nsteps):
+        nel = H.etrs_step(p, occ, dt, A_t=A, A_tdt=A, rho=rho, want_nel=True)
+        ref, rref, nref = oh.etrs_step(ref, occ, dt, A, A, want_rho=True, nthreads=NT)
+    assert rel_err(p.cpu().numpy(), ref.T) < 1e-10
+    assert rel_err(rho.cpu().numpy(), rref) < 1e-10
+    assert abs(nel - nref) < 1e-10 * nref
+
+
+def test_etrs_time_dependent_vector_potential(cuda):
+    cell, b, H, oft, oh, psi = setup("t12b")
+    occ = synth.occupations(cell)
+    dt = 0.05
+    torch = _torch()
+    p = dev(psi)
+    ref = psi.T.copy()
+    for k in range(2):
+        A0 = np.array([0.0, 0.02 * k, 0.01 + 0.005 * k])
+        A1 = np.array([0.0, 0.02 * (k + 1), 0.01 + 0.005 * (k + 1)])
+        H.etrs_step(p, occ, dt, A_t=A0, A_tdt=A1)
+        ref, _, _ = oh.etrs_step(ref, occ, dt, A0, A1, nthreads=NT)
+    assert rel_err(p.cpu().numpy(), ref.T) < 1e-10
+
+
+def test_etrs_mixed_error_vs_fp64_oracle(cuda):
+    cell, b, H, oft, oh, psi = setup("t12", prec="mixed")
+    occ = synth.occupations(cell)
+    A = synth.kick()
+    torch = _torch()
+    p = dev(psi)
+    ref = psi.T.copy()
+    for _ in range(3):
+        H.etrs_step(p, occ, 0.05, A_t=A, A_tdt=A)
+        ref, _, _ = oh.etrs_step(ref, occ, 0.05, A, A, nthreads=NT)
+    err = rel_err(p.cpu().numpy(), ref.T)
+    assert err < 5e-5, err
+
+
+def test_unsupported_and_too_small_grids(cuda):
+    b = Q.Basis(12.0, 10.0)
+    with pytest.raises(Q.QbgError, match="unsupported"):
+        Q.FourierTransform(b, 34, 32, 32)   # 34 = 2*17
+    with pytest.raises(Q.QbgError, match="invalid"):
+        Q.FourierTransform(b, 16, 16, 16)   # sphere does not fit
