@@ -1,0 +1,415 @@
+#!/usr/bin/env python3
+"""ETRS steps/s on the 216-atom cell: mixed precision vs the plain FP64 form.
+
+One "step" is one ETRS step of ExponentialWavefunctionStepper (preupdate +
+update: three 4th-order Taylor exponentials = 12 H|psi> applications, plus
+the density of the predicted state) over all 432 states of the synthetic
+216-atom cell (L = 30 bohr, ecut 50 Ry, 120^3 grid, 161 235 full-sphere
+plane waves, 9 KB projectors per atom), delta-kicked by A = (0, 0, 0.01).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is whole-job ETRS steps/s of the
+mixed form with psi resident in HBM (psi is 1.1 GB, far larger than L2, so
+no flush is needed between steps); `e2e` is the same step through the
+public API with psi copied in from pinned host memory and psi(t+dt) plus
+the current J read back every step.  `fp64_gpu` times the plain FP64 form
+on the same cell.  With N > 1 each rank propagates its own replica (no
+data-path collective; weak scaling).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "TDDFT ETRS steps/s (216 at.) mixed vs FP64 GPU at <=1e-8 dipole rel err"
+UNIT = "steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--dt", type=float, default=0.05)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--fp64-warmup", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-states", type=int, default=16)
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--chunk", type=int, default=0)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------ distributed
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------ clocks
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = float(parts[1])
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "power_w_median": float(np.median(power)) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ------------------------------------------------------------ system
+def make_system(cfg, precision, psi_np=None, chunk=0):
+    import torch
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    cell = synth.make_cell(cfg)
+    basis = Q.Basis(cell.L, cell.ecut)
+    H = Q.Hamiltonian(basis, *cell.grid, precision=precision)
+    if chunk:
+        H.set_chunk(chunk)
+    H.set_vlocal(synth.vlocal(cell))
+    H.set_nonlocal(synth.species(cell))
+    if psi_np is None:
+        psi_np = make_psi(cell, basis)
+    return cell, basis, H, psi_np
+
+
+def make_psi(cell, basis):
+    """Seeded random states, Gram-orthonormalised in FP64 on the device."""
+    import torch
+    rng = np.random.default_rng(cell.seed + 7)
+    n, ngw = cell.nst, basis.ngw
+    env = torch.from_numpy(np.exp(-basis.kpg2 / 8.0)).cuda()
+    c = torch.empty((n, ngw), dtype=torch.complex128, device="cuda")
+    for s0 in range(0, n, 64):
+        s1 = min(n, s0 + 64)
+        blk = rng.standard_normal((s1 - s0, ngw)) + 1j * rng.standard_normal((s1 - s0, ngw))
+        c[s0:s1] = torch.from_numpy(blk).cuda() * env
+    S = c.conj() @ c.T
+    L = torch.linalg.cholesky(S)
+    out = torch.linalg.solve_triangular(L.conj(), c, upper=False)
+    return out
+
+
+def time_etrs(H, p, occ, dt, A, steps, warmup, stream):
+    import torch
+    for _ in range(warmup):
+        H.etrs_step(p, occ, dt, A_t=A, A_tdt=A, stream=stream)
+    torch.cuda.synchronize()
+    l0 = H.launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        H.etrs_step(p, occ, dt, A_t=A, A_tdt=A, stream=stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), H.launches() - l0
+
+
+# ------------------------------------------------------------ roofline
+def phase_units(H, cell, basis, nst):
+    """Algorithmic bytes (HBM) or flops per launch of each phase."""
+    P = H.nproj if hasattr(H, "nproj") else None
+    n0, n1, n2 = cell.grid
+    ngw, nrods = basis.ngw, basis.nrods
+    nband = 2 * (max(abs(basis.idxmin[1]), abs(basis.idxmax[1])) + 1)
+    cs = 8 if H.precision == "mixed" else 16      # complex element bytes
+    rs = 4 if H.precision == "mixed" else 8       # real element bytes
+    chunk = H.chunk
+    return dict(
+        fnl_gemm=("flop", 8.0 * nproj_of(cell) * ngw * nst),
+        enl_hpsi=("flop", 8.0 * nproj_of(cell) * ngw * nst),
+        ft_z_bwd=("byte", chunk * (ngw * cs + n2 * nrods * cs)),
+        ft_x_bwd=("byte", chunk * n2 * (nrods * cs + nband * n0 * cs)),
+        ft_y_vloc=("byte", chunk * n2 * (2 * nband * n0 * cs) + n0 * n1 * n2 * rs),
+        ft_x_fwd=("byte", chunk * n2 * (nrods * cs + nband * n0 * cs)),
+        ft_z_fwd=("byte", chunk * (n2 * nrods * cs + 3 * ngw * cs + 2 * ngw * 16)),
+    )
+
+
+def nproj_of(cell):
+    return cell.natoms * (cell.lmax + 1) ** 2
+
+
+# ------------------------------------------------------------ CPU baseline
+def cpu_baseline(cfg, nsample, reps=1):
+    """The CPU oracle (plain-C restatement of the reference path, OpenMP over
+    states) on a bounded sample: H|psi> and the density of `nsample` states of
+    the full cell; one ETRS step is extrapolated as 12 H + 1 density over
+    all states (both linear in the number of states)."""
+    from oracle import oracle as O
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    cell = synth.make_cell(cfg)
+    b = O.Basis(Q.cubic_cell(cell.L), cell.ecut)
+    ft = O.FT(b, *cell.grid)
+    v = synth.vlocal(cell)
+    ham = O.Ham(ft, v, synth.species(cell))
+    ham.set_A(synth.kick())
+    rng = np.random.default_rng(5)
+    c = (rng.standard_normal((b.ngw, nsample)) + 1j * rng.standard_normal((b.ngw, nsample)))
+    c = np.asfortranarray(c * np.exp(-b.kpg2 / 8)[:, None])
+    occ = np.full(nsample, 2.0)
+    cores = os.cpu_count() or 1
+    th = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        ham.hpsi(c, occ, nthreads=cores)
+        t1 = time.perf_counter()
+        O.update_density(ft, c, occ, nthreads=cores)
+        t2 = time.perf_counter()
+        th.append((t1 - t0, t2 - t1))
+    th = np.array(th)
+    t_h, t_d = float(th[:, 0].min()), float(th[:, 1].min())
+    scale = cell.nst / nsample
+    step_s = (12 * t_h + t_d) * scale
+    return {"value": 1.0 / step_s, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": (f"oracle H|psi> ({t_h:.2f} s) + density ({t_d:.2f} s) of {nsample} of "
+                       f"{cell.nst} states of the full {cfg} cell, {cores} threads; ETRS step "
+                       f"= (12 H + 1 density) x {scale:.0f}")}
+
+
+# ------------------------------------------------------------ arms
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    K, W = max(1, args.steps), max(0, args.warmup)
+    vals = []
+    res = None
+    for i in range(W + K):
+        res = cpu_baseline(args.config, args.cpu_states)
+        if i >= W:
+            vals.append(res["value"])
+    v = float(np.median(vals))
+    res["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"{args.config}: 216-atom cell, L=30, 50 Ry, 120^3, 432 states, "
+                                   f"ETRS dt={args.dt}, sampled on {args.cpu_states} states"},
+            "cpu_baseline": res,
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    cell, basis, H, psi = make_system(args.config, "mixed", chunk=args.chunk)
+    occ = synth.occupations(cell)
+    A = synth.kick()
+    H.set_vector_potential(A)
+    p = psi.clone()
+    barrier(world)
+    clocks = Clocks(local)
+    clocks.start()
+    ms, launches = time_etrs(H, p, occ, args.dt, A, args.steps, args.warmup, stream)
+    clk = clocks.stop()
+    barrier(world)
+    ms_max = allreduce_max(ms, world)
+    value = world * args.steps / (ms_max / 1000.0)
+
+    # per-phase device time of one H application (profiled: launches run alone)
+    hp = torch.empty_like(p)
+    H.profile(True)
+    H.hpsi(p, hp, occ, stream=stream)
+    prof = H.profile_read()
+    H.profile(False)
+    units = phase_units(H, cell, basis, cell.nst)
+    dom = max(units, key=lambda k: prof[k][0])
+    tot_ms, nl = prof[dom]
+    kind, amount = units[dom]
+    per_launch_s = tot_ms / 1000.0 / max(nl, 1)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    if kind == "flop":
+        bound, unit_r = "fp32_fma" if True else "tensor", "TFLOP/s"
+        achieved = amount / per_launch_s / 1e12
+        peak = 72.2  # measured FFMA peak on this GB300 (profiles/peaks_gb300.txt)
+    else:
+        bound, unit_r = "hbm", "GB/s"
+        per_launch_amount = amount
+        achieved = per_launch_amount / per_launch_s / 1e9
+        peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(HERE, "profiles", "traffic.json")))
+        if dom in tr and tr[dom].get("config") == args.config:
+            traffic = tr[dom]["bytes_per_launch"]
+    except (OSError, ValueError):
+        pass
+    roofline = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
+                "unit": unit_r, "frac": achieved / peak, "traffic": traffic,
+                "per_launch_ms": per_launch_s * 1e3,
+                "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]}}
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.skip_e2e:
+        nbytes = p.numel() * p.element_size()
+        h_in = torch.empty(p.shape, dtype=p.dtype, pin_memory=True)
+        h_in.copy_(psi)
+        h_out = torch.empty_like(h_in, pin_memory=True)
+        J = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            p.copy_(h_in, non_blocking=True)
+            H.etrs_step(p, occ, args.dt, A_t=A, A_tdt=A, stream=stream)
+            J = H.current(p, occ, float(occ.sum()), stream=stream)
+            h_out.copy_(p, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        e2e_ms = e0.elapsed_time(e1)
+        e2e_ms = allreduce_max(e2e_ms, world)
+        e2e = {"value": world * args.e2e_steps / (e2e_ms / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes + 24,
+               "steps": args.e2e_steps, "wall_s": wall, "J_last": list(map(float, J))}
+        del h_in, h_out
+
+    # plain FP64 form on the same cell
+    fp64 = None
+    if not args.skip_fp64:
+        del H
+        torch.cuda.empty_cache()
+        _, _, H64, _ = make_system(args.config, "fp64", psi_np=psi)
+        H64.set_vector_potential(A)
+        p64 = psi.clone()
+        ms64, _ = time_etrs(H64, p64, occ, args.dt, A, args.fp64_steps, args.fp64_warmup, stream)
+        ms64 = allreduce_max(ms64, world)
+        fp64 = {"value": world * args.fp64_steps / (ms64 / 1000.0), "unit": UNIT,
+                "steps": args.fp64_steps, "warmup": args.fp64_warmup}
+        H64.profile(True)
+        H64.hpsi(p64, hp, occ, stream=stream)
+        fp64["phases_ms_per_H"] = {k: round(v[0], 3) for k, v in H64.profile_read().items() if v[1]}
+        H64.profile(False)
+        del H64, p64
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        cpu = cpu_baseline(args.config, args.cpu_states)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "mixed: f32 transforms + f32 projector GEMMs, f64 Taylor sum/reductions",
+                "data": "synthetic (seeded cell, random orthonormal states)",
+                "config": {"workload": f"{args.config}: 216 atoms, L=30 bohr, ecut 50 Ry, grid "
+                                       f"{cell.grid[0]}^3, {basis.ngw} PW (full sphere), "
+                                       f"{cell.nst} states, {nproj_of(cell)} KB projectors, "
+                                       f"ETRS dt={args.dt}, delta kick A_z=0.01",
+                           "l2": "inputs (psi 1.1 GB) larger than L2; no flush",
+                           "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
+                "gpu_launches": launches, "clocks": clk, "roofline": roofline,
+                "e2e": e2e, "fp64_gpu": fp64, "cpu_baseline": cpu}
+        if fp64:
+            line["mixed_over_fp64"] = value / fp64["value"]
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -170,9 +170,19 @@ qbg_status qbg_etrs_step(qbg_plan* plan, double* psi, int ld, int nst,
                          const double* A_tdt, double* rho_mid, double* nel,
                          void* stream);
 
-/* Number of this library's kernel launches issued since plan creation
- * (instrumentation for benchmarks). */
+/* ---- Instrumentation (no reference counterpart beyond its TimerMap,
+ *      NonLocalPotential.cc:54, EhrenSampleStepper.cc:1136-1149) ------- */
+/* Number of this library's kernel launches issued since plan creation. */
 qbg_status qbg_launch_count(const qbg_plan* plan, long long* count);
+/* enable != 0: bracket every kernel launch with CUDA events on its stream
+ * and accumulate per-phase device time (each launch then runs alone); the
+ * accumulators are reset by every call. */
+qbg_status qbg_profile(qbg_plan* plan, int enable);
+/* ms[i], launches[i] for phases i < n (qbg_phase_name(i) gives the name;
+ * there are 12 phases). */
+qbg_status qbg_profile_read(const qbg_plan* plan, double* ms,
+                            long long* launches, int n);
+const char* qbg_phase_name(int phase);
 
 #ifdef __cplusplus
 }

@@ -630,9 +630,11 @@ double qbo_nl_apply(const qbo_ham* h, const double* c, int ld, int nst,
       const int nblk = ia1 - ia0;
       const int nprna = nblk * sp->npr;
       double* anl = (double*)malloc(sizeof(double) * 2 * (size_t)ng * nprna);
-      for (int ipr = 0; ipr < sp->npr; ++ipr)
-        for (int ia = 0; ia < nblk; ++ia)
-          qbo_anl_column(h, sp, ipr, ia0 + ia, anl + 2 * (size_t)ng * (ia + ipr * nblk));
+#pragma omp parallel for num_threads(nthreads) schedule(static)
+      for (int col = 0; col < nprna; ++col) {
+        const int ipr = col / nblk, ia = col % nblk;
+        qbo_anl_column(h, sp, ipr, ia0 + ia, anl + 2 * (size_t)ng * (ia + ipr * nblk));
+      }
       double* fnl = (double*)malloc(sizeof(double) * 2 * (size_t)nprna * nst);
       /* fnl = anl^H c, reference ZGEMM('C','N') summation order */
 #pragma omp parallel for num_threads(nthreads) schedule(static)

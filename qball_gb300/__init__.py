@@ -56,7 +56,11 @@ ABI = {
     "qbg_current": [_P, _P, _I, _I, _P, _D, _P, _P],
     "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
     "qbg_launch_count": [_P, _P],
+    "qbg_profile": [_P, _I],
+    "qbg_profile_read": [_P, _P, _P, _I],
+    "qbg_phase_name": [_I],
 }
+NPHASE = 12
 
 
 class QbgError(RuntimeError):
@@ -81,7 +85,8 @@ def lib():
         for name, args in ABI.items():
             fn = getattr(L, name)
             fn.argtypes = args
-            fn.restype = ctypes.c_char_p if name in ("qbg_last_error", "qbg_version") else _I
+            fn.restype = (ctypes.c_char_p if name in ("qbg_last_error", "qbg_version", "qbg_phase_name")
+                          else _I)
         _lib = L
     return _lib
 
@@ -164,6 +169,7 @@ class FourierTransform:
         _check(lib().qbg_plan_create(ctypes.byref(d), int(np0), int(np1), int(np2), prec,
                                      ctypes.byref(h)), "qbg_plan_create")
         self.h = h
+        self.chunk = 16 if prec == QBG_PREC_MIXED else 8  # the plan's default
 
     def close(self):
         if getattr(self, "h", None):
@@ -176,8 +182,18 @@ class FourierTransform:
         except Exception:
             pass
 
+    def profile(self, enable=True):
+        _check(lib().qbg_profile(self.h, 1 if enable else 0), "qbg_profile")
+
+    def profile_read(self):
+        ms = np.zeros(NPHASE)
+        n = np.zeros(NPHASE, np.int64)
+        _check(lib().qbg_profile_read(self.h, _np_ptr(ms), _np_ptr(n), NPHASE), "qbg_profile_read")
+        return {lib().qbg_phase_name(i).decode(): (float(ms[i]), int(n[i])) for i in range(NPHASE)}
+
     def set_chunk(self, n):
         _check(lib().qbg_plan_set_chunk(self.h, int(n)), "qbg_plan_set_chunk")
+        self.chunk = int(n)
 
     def launches(self):
         c = ctypes.c_longlong()

@@ -329,6 +329,7 @@ static qbg_status run_z_bwd_(qbg_plan* p, const cplx<T>* c, int ldc, int ns, cud
   const size_t sm = smem_bytes<T>(d.n);
   QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
+  PhaseTimer pt(p, PH_Z_BWD, st);
   k_z_bwd<T, BIGP><<<grid, kThreads, sm, st>>>(c, ldc, (cplx<T>*)p->d_Z, p->d_rods, p->nrods, d);
   QBG_LAUNCHED(p);
   return QBG_OK;
@@ -344,6 +345,7 @@ static qbg_status run_x_(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
   const FFTLen<T> d = p->len[0].view<T>();
   const size_t sm = smem_bytes<T>(d.n);
   dim3 grid(p->np2 * ((p->nband + kTile - 1) / kTile), ns);
+  PhaseTimer pt(p, bwd ? PH_X_BWD : PH_X_FWD, st);
   if (bwd) {
     QBG_CUDA(prep(k_x_bwd<T, BIGP>, sm));
     k_x_bwd<T, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Z, (cplx<T>*)p->d_Y, p->nrods,
@@ -370,6 +372,8 @@ static qbg_status run_y_(qbg_plan* p, int ns, cplx<T>* f, const double* w, doubl
   const size_t sm = smem_bytes<T>(d.n);
   QBG_CUDA(prep(k_y<T, MODE, BIGP>, sm));
   dim3 grid(p->np2 * ((p->np0 + kTile - 1) / kTile), MODE == Y_DENSITY ? 1 : ns);
+  PhaseTimer pt(p, MODE == Y_VLOC ? PH_Y_VLOC : MODE == Y_DENSITY ? PH_Y_DENSITY
+                   : MODE == Y_BWD_STORE ? PH_Y_STORE : PH_Y_LOAD, st);
   const T* v = nullptr;
   if (MODE == Y_VLOC) v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vr32;
   k_y<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((cplx<T>*)p->d_Y, p->nband, p->np0, p->np2,
@@ -394,6 +398,7 @@ static qbg_status run_z_fwd_(qbg_plan* p, cplx<T>* out, int ldo, int ns, const c
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   const T scale = (T)(1.0 / (double)(p->np0 * p->np1 * p->np2));
   const T* kin = std::is_same<T, double>::value ? (const T*)p->d_kpg2A : (const T*)p->d_kpg2A32;
+  PhaseTimer pt(p, PH_Z_FWD, st);
   k_z_fwd<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
                                                     p->d_rods, p->nrods, d, scale, psi, ldp,
                                                     kin, out_init, acc, lda, fac);

@@ -41,6 +41,14 @@ struct LenTables {
   template <typename T> FFTLen<T> view() const;
 };
 
+// Timed phases (names follow the reference's TimerMap keys where one exists:
+// "fnl_gemm", "enl_hpsi" in NonLocalPotential.cc:2059-2170).
+enum Phase {
+  PH_FNL_GEMM = 0, PH_FNL_REDUCE, PH_ENL_HPSI, PH_Z_BWD, PH_X_BWD, PH_Y_VLOC,
+  PH_X_FWD, PH_Z_FWD, PH_Y_DENSITY, PH_Y_STORE, PH_Y_LOAD, PH_MISC, PH_COUNT
+};
+extern const char* const kPhaseName[PH_COUNT];
+
 // Per-rod table entry: G offset of the rod's first coefficient, rod length,
 // lmin, grid x index, band row index.
 struct RodInfo {
@@ -100,6 +108,11 @@ struct qbg_plan {
   double* d_red = nullptr; size_t red_bytes = 0;     // reduction partials
   double* d_rho = nullptr; size_t rho_bytes = 0;     // ETRS density scratch
   double* h_red = nullptr; size_t h_red_bytes = 0;   // pinned host copy
+  // phase profiler (off unless qbg_profile(plan, 1))
+  bool prof = false;
+  double prof_ms[qbg::PH_COUNT] = {0};
+  long long prof_n[qbg::PH_COUNT] = {0};
+  std::vector<double> occ_cache;  // last per-state factors uploaded to d_w[3]
   // ETRS work buffers
   void* d_w[4] = {nullptr, nullptr, nullptr, nullptr};
   size_t w_bytes[4] = {0, 0, 0, 0};
@@ -108,6 +121,35 @@ struct qbg_plan {
 namespace qbg {
 
 qbg_status ensure(void** p, size_t* cur, size_t need);
+
+// Brackets one kernel launch with CUDA events when the plan's profiler is on
+// (the stream is synchronised at the end of the bracket, so profiled runs
+// measure each kernel alone).
+struct PhaseTimer {
+  qbg_plan* p;
+  int ph;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr, b = nullptr;
+  PhaseTimer(qbg_plan* p_, int ph_, cudaStream_t st_) : p(p_), ph(ph_), st(st_) {
+    if (p->prof) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, st);
+    }
+  }
+  ~PhaseTimer() {
+    if (p->prof) {
+      cudaEventRecord(b, st);
+      cudaEventSynchronize(b);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, a, b);
+      p->prof_ms[ph] += ms;
+      p->prof_n[ph] += 1;
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  }
+};
 qbg_status ensure_host(double** p, size_t* cur, size_t need);
 
 // transforms (qbg_fft.cu); T = double or float.  Pointers are device.

@@ -357,17 +357,26 @@ qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int n
   if (s) return s;
   s = ensure(&p->d_fnl, &p->fnl_bytes, (size_t)P * nst * sizeof(cplx<T>));
   if (s) return s;
-  k_fnl<T><<<dim3(mt, nt, split), 256, 0, st>>>(anl, p->ngw, P, psi, ld, nst,
-                                                 (double2*)p->d_fpart, kchunk);
-  QBG_LAUNCHED(p);
+  {
+    PhaseTimer pt(p, PH_FNL_GEMM, st);
+    k_fnl<T><<<dim3(mt, nt, split), 256, 0, st>>>(anl, p->ngw, P, psi, ld, nst,
+                                                   (double2*)p->d_fpart, kchunk);
+    QBG_LAUNCHED(p);
+  }
   const size_t total = (size_t)P * nst;
   const int rb = (int)((total + 255) / 256);
-  k_fnl_reduce<T><<<rb, 256, 0, st>>>((const double2*)p->d_fpart, split, P, nst, p->d_pwt,
-                                      d_occ, (cplx<T>*)p->d_fnl, enl_part);
-  QBG_LAUNCHED(p);
-  k_nl_hpsi<T><<<dim3((p->ngw + GT - 1) / GT, nt), 256, 0, st>>>(
-      anl, p->ngw, P, (const cplx<T>*)p->d_fnl, nst, out, ld);
-  QBG_LAUNCHED(p);
+  {
+    PhaseTimer pt(p, PH_FNL_REDUCE, st);
+    k_fnl_reduce<T><<<rb, 256, 0, st>>>((const double2*)p->d_fpart, split, P, nst, p->d_pwt,
+                                        d_occ, (cplx<T>*)p->d_fnl, enl_part);
+    QBG_LAUNCHED(p);
+  }
+  {
+    PhaseTimer pt(p, PH_ENL_HPSI, st);
+    k_nl_hpsi<T><<<dim3((p->ngw + GT - 1) / GT, nt), 256, 0, st>>>(
+        anl, p->ngw, P, (const cplx<T>*)p->d_fnl, nst, out, ld);
+    QBG_LAUNCHED(p);
+  }
   return QBG_OK;
 }
 

@@ -14,6 +14,10 @@ namespace qbg {
 
 static thread_local std::string g_err;
 
+const char* const kPhaseName[PH_COUNT] = {
+    "fnl_gemm", "fnl_reduce", "enl_hpsi", "ft_z_bwd", "ft_x_bwd", "ft_y_vloc",
+    "ft_x_fwd", "ft_z_fwd", "ft_y_density", "ft_y_store", "ft_y_load", "misc"};
+
 void set_error(const char* fmt, ...) {
   char buf[512];
   va_list ap;
@@ -499,6 +503,33 @@ qbg_status qbg_plan_set_chunk(qbg_plan* p, int states) {
   p->chunk = states;
   return QBG_OK;
 }
+
+qbg_status qbg_profile(qbg_plan* p, int enable) {
+  if (!p) {
+    set_error("qbg_profile: null plan");
+    return QBG_ERR_INVALID;
+  }
+  p->prof = enable != 0;
+  for (int i = 0; i < PH_COUNT; ++i) {
+    p->prof_ms[i] = 0.0;
+    p->prof_n[i] = 0;
+  }
+  return QBG_OK;
+}
+
+qbg_status qbg_profile_read(const qbg_plan* p, double* ms, long long* launches, int n) {
+  if (!p || n < 0 || (n > 0 && (!ms || !launches))) {
+    set_error("qbg_profile_read: invalid argument");
+    return QBG_ERR_INVALID;
+  }
+  for (int i = 0; i < n && i < PH_COUNT; ++i) {
+    ms[i] = p->prof_ms[i];
+    launches[i] = p->prof_n[i];
+  }
+  return QBG_OK;
+}
+
+const char* qbg_phase_name(int i) { return (i >= 0 && i < PH_COUNT) ? kPhaseName[i] : ""; }
 
 qbg_status qbg_launch_count(const qbg_plan* p, long long* count) {
   if (!p || !count) {
