@@ -1,0 +1,97 @@
+"""Dipole accuracy of the precision forms against the plain FP64 form.
+
+    python -m qball_gb300.accuracy --config c2 --nst 32 --steps 200
+
+Propagates the same delta-kicked state with each precision form through the
+C ABI and records the total electronic current J(t) after every ETRS step
+(CurrentDensity::update_current, CurrentDensity.cc:39-106, G-space form).
+The dipole is d(t) = integral_0^t J dt' (trapezoid, FP64).  Reported per
+form: max_t |d(t) - d64(t)| / max_t |d64(t)| for the kick direction and for
+the vector norm, and the final relative wavefunction difference.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def run_form(precision, cell, basis, psi0, occ, A, dt, steps, chunk=0):
+    import torch
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    H = Q.Hamiltonian(basis, *cell.grid, precision=precision)
+    if chunk:
+        H.set_chunk(chunk)
+    H.set_vlocal(synth.vlocal(cell))
+    H.set_nonlocal(synth.species(cell))
+    H.set_vector_potential(A)
+    p = psi0.clone()
+    nel = float(occ.sum())
+    J = [H.current(p, occ, nel)]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        H.etrs_step(p, occ, dt, A_t=A, A_tdt=A)
+        J.append(H.current(p, occ, nel))
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    J = np.array(J)
+    d = np.zeros_like(J)
+    for k in range(1, len(J)):
+        d[k] = d[k - 1] + 0.5 * dt * (J[k - 1] + J[k])
+    H.close()
+    return dict(J=J, d=d, psi=p, seconds=el)
+
+
+def main():
+    import torch
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    sys.path.insert(0, os.path.dirname(HERE))
+    from bench import make_psi  # seeded state generator shared with bench.py
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--nst", type=int, default=0)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--dt", type=float, default=0.05)
+    ap.add_argument("--forms", default="fp64,mixed")
+    ap.add_argument("--out", default="")
+    args = ap.parse_args()
+    kw = {"nst": args.nst} if args.nst else {}
+    cell = synth.make_cell(args.config, **kw)
+    basis = Q.Basis(cell.L, cell.ecut)
+    psi0 = make_psi(cell, basis)
+    occ = synth.occupations(cell)
+    A = synth.kick()
+    res = {}
+    for form in args.forms.split(","):
+        res[form] = run_form(form, cell, basis, psi0, occ, A, args.dt, args.steps)
+    ref = res["fp64"]
+    dref = ref["d"]
+    scale_z = np.abs(dref[:, 2]).max()
+    scale_n = np.linalg.norm(dref, axis=1).max()
+    report = {"config": args.config, "nst": cell.nst, "steps": args.steps, "dt": args.dt,
+              "kick": list(A), "d64_final": list(map(float, dref[-1])), "forms": {}}
+    for form, r in res.items():
+        dd = r["d"] - dref
+        rel_z = float(np.abs(dd[:, 2]).max() / scale_z)
+        rel_n = float(np.linalg.norm(dd, axis=1).max() / scale_n)
+        pd = float(((r["psi"] - ref["psi"]).abs().pow(2).sum().sqrt()
+                    / ref["psi"].abs().pow(2).sum().sqrt()).item())
+        report["forms"][form] = {"dipole_rel_err_z": rel_z, "dipole_rel_err_norm": rel_n,
+                                 "psi_rel_err_final": pd, "seconds": r["seconds"],
+                                 "steps_per_s": args.steps / r["seconds"]}
+    print(json.dumps(report), flush=True)
+    if args.out:
+        np.savez(args.out, **{f"{k}_d": v["d"] for k, v in res.items()},
+                 **{f"{k}_J": v["J"] for k, v in res.items()})
+
+
+if __name__ == "__main__":
+    main()

@@ -39,7 +39,7 @@ template <typename T> __device__ __forceinline__ cplx<T> czero() {
 // along z, write Z[s][z][rod].
 template <typename T, bool BIGP>
 __global__ void __launch_bounds__(kThreads)
-k_z_bwd(const cplx<T>* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
+k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
         const RodInfo* __restrict__ rods, int nrods, FFTLen<T> d) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -48,7 +48,7 @@ k_z_bwd(const cplx<T>* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
   C* B = A + kTile * ls;
   const int r0 = blockIdx.x * kTile;
   const int nl = min(kTile, nrods - r0);
-  const C* ps = psi + (size_t)blockIdx.y * ld;
+  const double2* ps = psi + (size_t)blockIdx.y * ld;
   for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -57,7 +57,11 @@ k_z_bwd(const cplx<T>* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
     for (int i = lane; i < ri.size; i += 32) {
       int z = ri.lmin + i;
       if (z < 0) z += n2;
-      A[rl * ls + z] = ps[ri.first + i];
+      const double2 v = ps[ri.first + i];
+      C c;
+      c.x = (T)v.x;
+      c.y = (T)v.y;
+      A[rl * ls + z] = c;
     }
   }
   __syncthreads();
@@ -75,9 +79,9 @@ k_z_bwd(const cplx<T>* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
 //   1 hpsi        o = (o_nl + kin*psi) + val; out[g] = o; acc[g] += fac*o
 template <typename T, int MODE, bool BIGP>
 __global__ void __launch_bounds__(kThreads)
-k_z_fwd(const cplx<T>* __restrict__ Z, cplx<T>* __restrict__ out, int ldo,
+k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
         const RodInfo* __restrict__ rods, int nrods, FFTLen<T> d, T scale,
-        const cplx<T>* psi, int ldp, const T* __restrict__ kpg2,
+        const double2* psi, int ldp, const double* __restrict__ kpg2,
         int out_init, double2* acc, int lda, double2 fac) {
   // psi and acc may alias (the Taylor series is accumulated into the input
   // of the first H application); each element is read before it is written
@@ -98,22 +102,23 @@ k_z_fwd(const cplx<T>* __restrict__ Z, cplx<T>* __restrict__ out, int ldo,
   __syncthreads();
   const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  C* os = out + (size_t)s * ldo;
+  double2* os = out + (size_t)s * ldo;
   for (int rl = warp; rl < nl; rl += nw) {
     const RodInfo ri = rods[r0 + rl];
     for (int i = lane; i < ri.size; i += 32) {
       int z = ri.lmin + i;
       if (z < 0) z += n2;
-      C v = R[rl * ls + z];
-      v.x *= scale;
-      v.y *= scale;
+      C vt = R[rl * ls + z];
+      vt.x *= scale;
+      vt.y *= scale;
+      const double2 v = make_double2((double)vt.x, (double)vt.y);
       const int g = ri.first + i;
       if (MODE == 0) {
         os[g] = v;
       } else {
-        const C c = psi[(size_t)s * ldp + g];
-        const T x = T(0.5) * kpg2[g];
-        C o = out_init ? os[g] : czero<T>();
+        const double2 c = psi[(size_t)s * ldp + g];
+        const double x = 0.5 * kpg2[g];
+        double2 o = out_init ? os[g] : make_double2(0.0, 0.0);
         o.x = o.x + x * c.x;
         o.y = o.y + x * c.y;
         o.x = o.x + v.x;
@@ -205,7 +210,7 @@ template <typename T, int MODE, bool BIGP>
 __global__ void __launch_bounds__(kThreads)
 k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
     const int* __restrict__ band_y, const T* __restrict__ v,
-    cplx<T>* __restrict__ f, const double* __restrict__ w, int nstates,
+    double2* __restrict__ f, const double* __restrict__ w, int nstates,
     double* __restrict__ rho, int rho_accumulate, FFTLen<T> d) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -226,10 +231,14 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
     C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
     C* R;
     if (MODE == Y_FWD_LOAD) {
-      const C* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
+      const double2* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
       for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
         const int cl = it % nl, y = it / nl;
-        A[cl * ls + y] = fs[(size_t)y * n0 + x0 + cl];
+        const double2 fv = fs[(size_t)y * n0 + x0 + cl];
+        C c;
+        c.x = (T)fv.x;
+        c.y = (T)fv.y;
+        A[cl * ls + y] = c;
       }
       __syncthreads();
       R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
@@ -258,10 +267,11 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
       R = fft_lines<-1, T, BIGP>(R, other, nl, ls, d);
     }
     if (MODE == Y_BWD_STORE) {
-      C* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
+      double2* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
       for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
         const int cl = it % nl, y = it / nl;
-        fs[(size_t)y * n0 + x0 + cl] = R[cl * ls + y];
+        const C c = R[cl * ls + y];
+        fs[(size_t)y * n0 + x0 + cl] = make_double2((double)c.x, (double)c.y);
       }
     } else if (MODE == Y_DENSITY) {
       const double ws = w[s];
@@ -324,7 +334,7 @@ static bool big_prime(const LenTables& L) {
 }
 
 template <typename T, bool BIGP>
-static qbg_status run_z_bwd_(qbg_plan* p, const cplx<T>* c, int ldc, int ns, cudaStream_t st) {
+static qbg_status run_z_bwd_(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st) {
   const FFTLen<T> d = p->len[2].view<T>();
   const size_t sm = smem_bytes<T>(d.n);
   QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
@@ -335,7 +345,7 @@ static qbg_status run_z_bwd_(qbg_plan* p, const cplx<T>* c, int ldc, int ns, cud
   return QBG_OK;
 }
 template <typename T>
-static qbg_status run_z_bwd(qbg_plan* p, const cplx<T>* c, int ldc, int ns, cudaStream_t st) {
+static qbg_status run_z_bwd(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st) {
   return big_prime(p->len[2]) ? run_z_bwd_<T, true>(p, c, ldc, ns, st)
                               : run_z_bwd_<T, false>(p, c, ldc, ns, st);
 }
@@ -366,7 +376,7 @@ static qbg_status run_x(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
 }
 
 template <typename T, int MODE, bool BIGP>
-static qbg_status run_y_(qbg_plan* p, int ns, cplx<T>* f, const double* w, double* rho,
+static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, double* rho,
                          int rho_acc, cudaStream_t st) {
   const FFTLen<T> d = p->len[1].view<T>();
   const size_t sm = smem_bytes<T>(d.n);
@@ -382,14 +392,14 @@ static qbg_status run_y_(qbg_plan* p, int ns, cplx<T>* f, const double* w, doubl
   return QBG_OK;
 }
 template <typename T, int MODE>
-static qbg_status run_y(qbg_plan* p, int ns, cplx<T>* f, const double* w, double* rho,
+static qbg_status run_y(qbg_plan* p, int ns, double2* f, const double* w, double* rho,
                         int rho_acc, cudaStream_t st) {
   return big_prime(p->len[1]) ? run_y_<T, MODE, true>(p, ns, f, w, rho, rho_acc, st)
                               : run_y_<T, MODE, false>(p, ns, f, w, rho, rho_acc, st);
 }
 
 template <typename T, int MODE, bool BIGP>
-static qbg_status run_z_fwd_(qbg_plan* p, cplx<T>* out, int ldo, int ns, const cplx<T>* psi,
+static qbg_status run_z_fwd_(qbg_plan* p, double2* out, int ldo, int ns, const double2* psi,
                              int ldp, int out_init, double2* acc, int lda, double2 fac,
                              cudaStream_t st) {
   const FFTLen<T> d = p->len[2].view<T>();
@@ -397,7 +407,7 @@ static qbg_status run_z_fwd_(qbg_plan* p, cplx<T>* out, int ldo, int ns, const c
   QBG_CUDA(prep(k_z_fwd<T, MODE, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   const T scale = (T)(1.0 / (double)(p->np0 * p->np1 * p->np2));
-  const T* kin = std::is_same<T, double>::value ? (const T*)p->d_kpg2A : (const T*)p->d_kpg2A32;
+  const double* kin = p->d_kpg2A;
   PhaseTimer pt(p, PH_Z_FWD, st);
   k_z_fwd<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
                                                     p->d_rods, p->nrods, d, scale, psi, ldp,
@@ -406,7 +416,7 @@ static qbg_status run_z_fwd_(qbg_plan* p, cplx<T>* out, int ldo, int ns, const c
   return QBG_OK;
 }
 template <typename T, int MODE>
-static qbg_status run_z_fwd(qbg_plan* p, cplx<T>* out, int ldo, int ns, const cplx<T>* psi,
+static qbg_status run_z_fwd(qbg_plan* p, double2* out, int ldo, int ns, const double2* psi,
                             int ldp, int out_init, double2* acc, int lda, double2 fac,
                             cudaStream_t st) {
   return big_prime(p->len[2])
@@ -421,7 +431,7 @@ static qbg_status run_z_fwd(qbg_plan* p, cplx<T>* out, int ldo, int ns, const cp
   } while (0)
 
 template <typename T>
-qbg_status local_hpsi(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int nst,
+qbg_status local_hpsi(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
                       bool out_init, double2* acc, int ldacc, double2 fac, cudaStream_t st) {
   const int ch = std::max(1, std::min(p->chunk, nst));
   QBG_TRY(ensure_scratch<T>(p, ch));
@@ -439,7 +449,7 @@ qbg_status local_hpsi(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int
 }
 
 template <typename T>
-qbg_status backward(qbg_plan* p, const cplx<T>* c, int ldc, cplx<T>* f, int nb, cudaStream_t st) {
+qbg_status backward(qbg_plan* p, const double2* c, int ldc, double2* f, int nb, cudaStream_t st) {
   const int ch = std::max(1, std::min(p->chunk, nb));
   QBG_TRY(ensure_scratch<T>(p, ch));
   for (int s0 = 0; s0 < nb; s0 += ch) {
@@ -452,7 +462,7 @@ qbg_status backward(qbg_plan* p, const cplx<T>* c, int ldc, cplx<T>* f, int nb, 
 }
 
 template <typename T>
-qbg_status forward(qbg_plan* p, cplx<T>* f, cplx<T>* c, int ldc, int nb, cudaStream_t st) {
+qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb, cudaStream_t st) {
   const int ch = std::max(1, std::min(p->chunk, nb));
   QBG_TRY(ensure_scratch<T>(p, ch));
   const double2 zero = make_double2(0.0, 0.0);
@@ -467,7 +477,7 @@ qbg_status forward(qbg_plan* p, cplx<T>* f, cplx<T>* c, int ldc, int nb, cudaStr
 }
 
 template <typename T>
-qbg_status density(qbg_plan* p, const cplx<T>* c, int ldc, int nst, const double* d_w,
+qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst, const double* d_w,
                    double* rho, cudaStream_t st) {
   const int ch = std::max(1, std::min(p->chunk, nst));
   QBG_TRY(ensure_scratch<T>(p, ch));
@@ -486,15 +496,13 @@ qbg_status density(qbg_plan* p, const cplx<T>* c, int ldc, int nst, const double
 
 template qbg_status local_hpsi<double>(qbg_plan*, const double2*, int, double2*, int, bool,
                                        double2*, int, double2, cudaStream_t);
-template qbg_status local_hpsi<float>(qbg_plan*, const float2*, int, float2*, int, bool,
+template qbg_status local_hpsi<float>(qbg_plan*, const double2*, int, double2*, int, bool,
                                       double2*, int, double2, cudaStream_t);
 template qbg_status backward<double>(qbg_plan*, const double2*, int, double2*, int, cudaStream_t);
-template qbg_status backward<float>(qbg_plan*, const float2*, int, float2*, int, cudaStream_t);
 template qbg_status forward<double>(qbg_plan*, double2*, double2*, int, int, cudaStream_t);
-template qbg_status forward<float>(qbg_plan*, float2*, float2*, int, int, cudaStream_t);
 template qbg_status density<double>(qbg_plan*, const double2*, int, int, const double*, double*,
                                     cudaStream_t);
-template qbg_status density<float>(qbg_plan*, const float2*, int, int, const double*, double*,
+template qbg_status density<float>(qbg_plan*, const double2*, int, int, const double*, double*,
                                    cudaStream_t);
 
 }  // namespace qbg

@@ -99,6 +99,9 @@ struct qbg_plan {
   double2* d_anl = nullptr;    // [nproj][ngw] FP64 projector table
   float2* d_anl32 = nullptr;   // [nproj][ngw] FP32 copy (mixed)
   bool nl_ready = false;
+  void* tc = nullptr;          // tensor-core projector tables (mixed)
+  bool check_every_step = true; // read the tensor-core status word after each step
+  int tc_nst_cleared = 0;
 
   // scratch (allocated lazily, grown as needed)
   void* d_Z = nullptr;  size_t Z_bytes = 0;   // [chunk][n2][nrods]
@@ -156,18 +159,20 @@ qbg_status ensure_host(double** p, size_t* cur, size_t need);
 // Hpsi local part for states [s0, s0+ns): out[g] = (out[g] + kin*psi[g]) +
 // fwd(v * bwd(psi))[g] (out holds the nonlocal part, or zero when
 // out_init == false); when acc != null: acc[g] += fac * out[g] (FP64).
+// T is the arithmetic type of the transforms; wavefunctions, H psi and the
+// accumulator are FP64 in memory.
 template <typename T>
-qbg_status local_hpsi(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out,
+qbg_status local_hpsi(qbg_plan* p, const double2* psi, int ld, double2* out,
                       int nst, bool out_init, double2* acc, int ldacc,
                       double2 fac, cudaStream_t st);
 template <typename T>
-qbg_status backward(qbg_plan* p, const cplx<T>* c, int ldc, cplx<T>* f,
+qbg_status backward(qbg_plan* p, const double2* c, int ldc, double2* f,
                     int nb, cudaStream_t st);
 template <typename T>
-qbg_status forward(qbg_plan* p, cplx<T>* f, cplx<T>* c, int ldc, int nb,
+qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb,
                    cudaStream_t st);
 template <typename T>
-qbg_status density(qbg_plan* p, const cplx<T>* c, int ldc, int nst,
+qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst,
                    const double* d_w, double* rho, cudaStream_t st);
 
 // nonlocal (qbg_nl.cu)
@@ -176,6 +181,14 @@ template <typename T>
 qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out,
                     int nst, const double* d_occ, double* enl_dev,
                     cudaStream_t st);
+
+// tensor-core projector GEMMs (qbg_tc.cu): psi, out FP64 [ld x nst]
+qbg_status tc_build(qbg_plan* p, cudaStream_t st);
+void tc_release(qbg_plan* p);
+qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
+                       const double* d_occ, double* enl_part, int* enl_blocks,
+                       cudaStream_t st);
+qbg_status tc_check_status(qbg_plan* p);
 
 // misc kernels (qbg_ops.cu)
 qbg_status update_kinetic(qbg_plan* p, cudaStream_t st);

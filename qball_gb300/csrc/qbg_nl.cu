@@ -138,6 +138,7 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
     atom0 += na;
   }
   p->nproj = (int)pd.size();
+  tc_release(p);
   if (p->d_ptau) cudaFree(p->d_ptau);
   if (p->d_pwt) cudaFree(p->d_pwt);
   if (p->d_anl) cudaFree(p->d_anl);
@@ -155,15 +156,9 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
   QBG_CUDA(cudaMemcpy(p->d_pwt, wt.data(), sizeof(double) * wt.size(), cudaMemcpyHostToDevice));
   const size_t n = (size_t)p->nproj * p->ngw;
   QBG_CUDA(cudaMalloc(&p->d_anl, sizeof(double2) * n));
-  const bool mixed = p->prec == QBG_PREC_MIXED;
-  if (mixed) QBG_CUDA(cudaMalloc(&p->d_anl32, sizeof(float2) * n));
   dim3 grid((p->ngw + 255) / 256, p->nproj);
-  if (mixed)
-    k_anl<true><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
-                                      d_pd, p->nproj, p->d_anl, p->d_anl32);
-  else
-    k_anl<false><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
-                                       d_pd, p->nproj, p->d_anl, nullptr);
+  k_anl<false><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
+                                     d_pd, p->nproj, p->d_anl, nullptr);
   p->launches++;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -386,7 +381,5 @@ int nl_reduce_blocks(const qbg_plan* p, int nst) {
 
 template qbg_status nl_apply<double>(qbg_plan*, const double2*, int, double2*, int,
                                      const double*, double*, cudaStream_t);
-template qbg_status nl_apply<float>(qbg_plan*, const float2*, int, float2*, int, const double*,
-                                    double*, cudaStream_t);
 
 }  // namespace qbg

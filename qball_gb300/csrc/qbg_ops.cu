@@ -108,15 +108,24 @@ static qbg_status upload_occ(qbg_plan* p, const double* occ, int nst, double sca
   return QBG_OK;
 }
 
-// H psi for a block of states in the plan's working precision T.  When acc
-// is set, acc += fac * (H psi) is fused into the last pass.
-template <typename T>
-static qbg_status hpsi_core(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int nst,
-                            const double* d_occ, double* enl_part, double2* acc, int ldacc,
-                            double2 fac, cudaStream_t st) {
+// H psi for a block of states (FP64 in and out).  The plain form runs the
+// transforms and projector GEMMs in FP64; the mixed form runs the transforms
+// in FP32 and the projector GEMMs on the tensor cores.  When acc is set,
+// acc += fac * (H psi) is fused into the last pass.
+static qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
+                            const double* d_occ, double* enl_part, int* enl_blocks,
+                            double2* acc, int ldacc, double2 fac, cudaStream_t st) {
   const bool nl = p->nproj > 0;
-  if (nl) QBG_TRY(nl_apply<T>(p, psi, ld, out, nst, d_occ, enl_part, st));
-  return local_hpsi<T>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
+  *enl_blocks = 0;
+  if (p->prec == QBG_PREC_FP64) {
+    if (nl) {
+      QBG_TRY(nl_apply<double>(p, psi, ld, out, nst, d_occ, enl_part, st));
+      *enl_blocks = nl_reduce_blocks(p, nst);
+    }
+    return local_hpsi<double>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
+  }
+  if (nl) QBG_TRY(tc_nl_apply(p, psi, ld, out, nst, d_occ, enl_part, enl_blocks, st));
+  return local_hpsi<float>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
 }
 
 static qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, const char* who) {
@@ -231,26 +240,13 @@ qbg_status qbg_hpsi(qbg_plan* p, const double* psi, int ld, double* hpsi, int ns
   QBG_TRY(ensure_nl(p, st));
   double* d_occ = nullptr;
   QBG_TRY(upload_occ(p, occ, nst, 1.0, &d_occ, st));
-  const int nb = p->nproj > 0 ? nl_reduce_blocks(p, nst) : 0;
-  QBG_TRY(ensure((void**)&p->d_red, &p->red_bytes, sizeof(double) * std::max(nb, 1)));
+  const int nbmax = p->nproj > 0 ? nl_reduce_blocks(p, nst) : 0;
+  QBG_TRY(ensure((void**)&p->d_red, &p->red_bytes, sizeof(double) * std::max(nbmax, 1)));
   const double2 zero = make_double2(0.0, 0.0);
-  if (p->prec == QBG_PREC_FP64) {
-    QBG_TRY(hpsi_core<double>(p, (const double2*)psi, ld, (double2*)hpsi, nst, d_occ,
-                              enl ? p->d_red : nullptr, nullptr, 0, zero, st));
-  } else {
-    const size_t need = sizeof(float2) * (size_t)ld * nst;
-    QBG_TRY(ensure(&p->d_w[0], &p->w_bytes[0], need));
-    QBG_TRY(ensure(&p->d_w[1], &p->w_bytes[1], need));
-    float2* a = (float2*)p->d_w[0];
-    float2* b = (float2*)p->d_w[1];
-    dim3 g((p->ngw + 255) / 256, nst);
-    k_cvt64to32<<<g, 256, 0, st>>>((const double2*)psi, ld, a, ld, p->ngw);
-    QBG_LAUNCHED(p);
-    QBG_TRY(hpsi_core<float>(p, a, ld, b, nst, d_occ, enl ? p->d_red : nullptr, nullptr, 0,
-                             zero, st));
-    k_cvt32to64<<<g, 256, 0, st>>>(b, ld, (double2*)hpsi, ld, p->ngw);
-    QBG_LAUNCHED(p);
-  }
+  int nb = 0;
+  QBG_TRY(hpsi_core(p, (const double2*)psi, ld, (double2*)hpsi, nst, d_occ,
+                    enl ? p->d_red : nullptr, &nb, nullptr, 0, zero, st));
+  if (p->prec == QBG_PREC_MIXED) QBG_TRY(tc_check_status(p));
   if (enl) {
     *enl = 0.0;
     if (nb > 0) {
@@ -283,15 +279,7 @@ static qbg_status sum_device(qbg_plan* p, const double* x, long long n, double* 
 static qbg_status density_any(qbg_plan* p, const double2* psi, int ld, int nst,
                               const double* d_w, double* rho, cudaStream_t st) {
   if (p->prec == QBG_PREC_FP64) return density<double>(p, psi, ld, nst, d_w, rho, st);
-  const size_t need = sizeof(float2) * (size_t)ld * std::max(nst, 1);
-  QBG_TRY(ensure(&p->d_w[0], &p->w_bytes[0], need));
-  float2* a = (float2*)p->d_w[0];
-  if (nst > 0) {
-    dim3 g((p->ngw + 255) / 256, nst);
-    k_cvt64to32<<<g, 256, 0, st>>>(psi, ld, a, ld, p->ngw);
-    QBG_LAUNCHED(p);
-  }
-  return density<float>(p, a, ld, nst, d_w, rho, st);
+  return density<float>(p, psi, ld, nst, d_w, rho, st);
 }
 
 qbg_status qbg_density(qbg_plan* p, const double* psi, int ld, int nst, const double* occ,
@@ -348,20 +336,13 @@ qbg_status qbg_current(qbg_plan* p, const double* psi, int ld, int nst, const do
 
 // exponential(1, dt1) of ExponentialWavefunctionStepper.cc:51-148: the
 // Taylor series is accumulated straight into psi (FP64); the four H
-// applications ping-pong between two work buffers.
+// applications ping-pong between two FP64 work buffers.
 static qbg_status exponential(qbg_plan* p, double2* psi, int ld, int nst, const double* d_occ,
                               double dt1, cudaStream_t st) {
   double f_re = 1.0, f_im = 0.0;
   const size_t n64 = sizeof(double2) * (size_t)ld * nst;
-  const size_t n32 = sizeof(float2) * (size_t)ld * nst;
-  const bool mixed = p->prec == QBG_PREC_MIXED;
-  QBG_TRY(ensure(&p->d_w[0], &p->w_bytes[0], mixed ? n32 : n64));
-  QBG_TRY(ensure(&p->d_w[1], &p->w_bytes[1], mixed ? n32 : n64));
-  if (mixed) {
-    dim3 g((p->ngw + 255) / 256, nst);
-    k_cvt64to32<<<g, 256, 0, st>>>(psi, ld, (float2*)p->d_w[0], ld, p->ngw);
-    QBG_LAUNCHED(p);
-  }
+  QBG_TRY(ensure(&p->d_w[0], &p->w_bytes[0], n64));
+  QBG_TRY(ensure(&p->d_w[1], &p->w_bytes[1], n64));
   for (int N = 1; N <= 4; ++N) {
     // factor1 *= -complex(0,1)*dt1/double(N)
     const double m_re = -0.0 * dt1 / (double)N, m_im = -1.0 * dt1 / (double)N;
@@ -369,15 +350,10 @@ static qbg_status exponential(qbg_plan* p, double2* psi, int ld, int nst, const 
     f_re = n_re;
     f_im = n_im;
     const double2 fac = make_double2(f_re, f_im);
-    if (mixed) {
-      const float2* in = (const float2*)p->d_w[(N - 1) & 1];
-      float2* out = (float2*)p->d_w[N & 1];
-      QBG_TRY(hpsi_core<float>(p, in, ld, out, nst, d_occ, nullptr, psi, ld, fac, st));
-    } else {
-      const double2* in = N == 1 ? psi : (const double2*)p->d_w[N & 1];
-      double2* out = (double2*)p->d_w[(N - 1) & 1];
-      QBG_TRY(hpsi_core<double>(p, in, ld, out, nst, d_occ, nullptr, psi, ld, fac, st));
-    }
+    const double2* in = N == 1 ? psi : (const double2*)p->d_w[N & 1];
+    double2* out = (double2*)p->d_w[(N - 1) & 1];
+    int nb;
+    QBG_TRY(hpsi_core(p, in, ld, out, nst, d_occ, nullptr, &nb, psi, ld, fac, st));
   }
   return QBG_OK;
 }
@@ -420,6 +396,7 @@ qbg_status qbg_etrs_step(qbg_plan* p, double* psi_, int ld, int nst, const doubl
   }
   if (A_tdt) QBG_TRY(qbg_set_vector_potential(p, A_tdt));
   QBG_TRY(exponential(p, psi, ld, nst, d_occ, dt1, st));
+  if (p->prec == QBG_PREC_MIXED && p->check_every_step) QBG_TRY(tc_check_status(p));
   return QBG_OK;
 }
 

@@ -362,6 +362,7 @@ qbg_status qbg_basis_fill(const double* a, double ecut, int* rod_h, int* rod_k,
 
 qbg_status qbg_plan_destroy(qbg_plan* p) {
   if (!p) return QBG_OK;
+  tc_release(p);
   for (auto& L : p->len) free_len(L);
   void* bufs[] = {p->d_rods, p->d_row_ptr, p->d_row_rod, p->d_row_x, p->d_band_y,
                   p->d_kpgx, p->d_kpg2A, p->d_kpg2A32, p->d_vr, p->d_vr32,

@@ -1,0 +1,716 @@
+// qbg_tc.cu -- projector GEMMs on the 5th-generation tensor cores (tcgen05).
+//
+// Mixed precision form of NonLocalPotential::energy (NonLocalPotential.cc:
+// 2059-2170).  Both complex GEMMs are rewritten as real GEMMs D = A B^T with
+// K-major operands:
+//   GEMM1  D[2P x nst]    = X1[2P x 2ngw]  * Psi[nst x 2ngw]^T   -> fnl
+//   GEMM2  D[2ngw x nst]  = X2[2ngw x 2P]  * Fnl[nst x 2P]^T     -> H psi (NL part)
+// where Psi and Fnl are the interleaved (re,im) views of the wavefunctions
+// and projections, and X1 (X2 = X1^T) interleaves anl so that one real dot
+// product yields the real or imaginary part (X1[2p][2g]=re, [2p][2g+1]=im,
+// [2p+1][2g]=-im, [2p+1][2g+1]=re).
+//
+// Precision: every operand row is scaled by a power of two and split into two
+// FP16 pieces (hi = fp16(x), lo = fp16(x - hi): 22 significant bits).  Three
+// products hi*hi + hi*lo + lo*hi run as kind::f16 MMAs (M=128, N=128, K=16)
+// accumulating in FP32 in tensor memory.  Every 256 K-elements the chunk sum
+// is folded into a compensated (hi, lo) FP32 pair that also lives in tensor
+// memory, so the total carries ~FP64-class accumulation error and FP32-class
+// operand error.
+//
+// Data movement: operands are pre-split into a tile-canonical layout in HBM
+// (each 128x32 block of a piece is one contiguous 8 KB image of the shared-
+// memory canonical K-major layout), so the producer warp moves them with 1-D
+// bulk async copies (cp.async.bulk, completion on an mbarrier).
+//
+// Warp roles (192 threads): warp 0 producer, warp 1 MMA issuer, warps 2-5
+// epilogue (tensor-memory lane quarters 2,3,0,1).  Every wait is bounded; a
+// timeout sets an error word, the CTA drains and frees its tensor memory.
+#include <algorithm>
+#include <cstdint>
+#include <cuda_fp16.h>
+#include <vector>
+
+#include "qbg_internal.h"
+
+namespace qbg {
+
+#define QBG_TRY_TC(x)             \
+  do {                            \
+    qbg_status s_ = (x);          \
+    if (s_ != QBG_OK) return s_;  \
+  } while (0)
+
+constexpr int TC_M = 128;          // rows per tile (A)
+constexpr int TC_N = 128;          // rows per tile (B) = MMA N
+constexpr int TC_KS = 32;          // K elements per pipeline stage
+constexpr int TC_STAGES = 4;
+constexpr int TC_CHUNK = 8;        // stages per tensor-memory chunk (K = 256)
+constexpr int TC_BLOCK_BYTES = TC_M * TC_KS * 2;   // 8 KB per piece per stage
+constexpr int TC_STAGE_BYTES = 4 * TC_BLOCK_BYTES; // A0 A1 B0 B1
+constexpr int TC_THREADS = 192;
+constexpr long long TC_SPIN = 1LL << 22;
+
+// byte offset of element (r, k) inside one 128x32 block image
+__host__ __device__ __forceinline__ int tc_canon(int r, int k) {
+  const int kk = k >> 4, kl = k & 15;
+  return kk * 4096 + (r >> 3) * 256 + (kl >> 3) * 128 + (r & 7) * 16 + (kl & 7) * 2;
+}
+
+// element offset (in halves) of (piece, row, k) in a tile-canonical array
+// with nRT row tiles and nKS K stages
+__host__ __device__ __forceinline__ size_t tc_index(int piece, int r, int k, int nRT, int nKS) {
+  const size_t blk = ((size_t)piece * nRT + (r >> 7)) * nKS + (k >> 5);
+  return blk * (TC_BLOCK_BYTES / 2) + (tc_canon(r & 127, k & 31) >> 1);
+}
+
+// --------------------------------------------------------------- splitting
+__device__ __forceinline__ void split2(float x, __half& hi, __half& lo) {
+  hi = __float2half_rn(x);
+  lo = __float2half_rn(x - __half2float(hi));
+}
+__device__ __forceinline__ void split2d(double x, __half& hi, __half& lo) {
+  hi = __double2half(x);
+  lo = __double2half(x - (double)__half2float(hi));
+}
+
+// exponent e with |x| * 2^-e < 2^14 for all |x| <= amax (0 when amax == 0)
+__device__ __forceinline__ int scale_exp(double amax) {
+  if (!(amax > 0.0)) return 0;
+  int e;
+  frexp(amax, &e);  // amax = f * 2^e, f in [0.5, 1)
+  return e - 14;
+}
+
+// per-projector and per-G maxima of |re|,|im| of anl[p][g]
+__global__ void k_anl_rowmax(const double2* __restrict__ anl, int nproj, int ngw,
+                             double* __restrict__ pmax) {
+  __shared__ double red[256];
+  const int p = blockIdx.x;
+  double m = 0.0;
+  for (int g = threadIdx.x; g < ngw; g += blockDim.x) {
+    const double2 a = anl[(size_t)p * ngw + g];
+    m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) pmax[p] = red[0];
+}
+
+__global__ void k_anl_colmax(const double2* __restrict__ anl, int nproj, int ngw,
+                             double* __restrict__ gmax) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= ngw) return;
+  double m = 0.0;
+  for (int p = 0; p < nproj; ++p) {
+    const double2 a = anl[(size_t)p * ngw + g];
+    m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
+  }
+  gmax[g] = m;
+}
+
+// X1 pieces: rows 2p+c, K = 2ngw; element values of the interleaved form
+__global__ void k_split_x1(const double2* __restrict__ anl, int nproj, int ngw,
+                           const double* __restrict__ pmax, __half* __restrict__ X1,
+                           int nRT, int nKS, float* __restrict__ rscale) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  const int e = scale_exp(pmax[p]);
+  if (g == 0) {
+    rscale[2 * p] = ldexpf(1.f, e);
+    rscale[2 * p + 1] = ldexpf(1.f, e);
+  }
+  if (g >= ngw) return;
+  const double2 a = anl[(size_t)p * ngw + g];
+  const double re = ldexp(a.x, -e), im = ldexp(a.y, -e);
+  const double v[4] = {re, im, -im, re};  // (2p,2g) (2p,2g+1) (2p+1,2g) (2p+1,2g+1)
+  for (int q = 0; q < 4; ++q) {
+    const int r = 2 * p + (q >> 1), k = 2 * g + (q & 1);
+    __half hi, lo;
+    split2d(v[q], hi, lo);
+    X1[tc_index(0, r, k, nRT, nKS)] = hi;
+    X1[tc_index(1, r, k, nRT, nKS)] = lo;
+  }
+}
+
+// X2 = X1^T pieces: rows m = 2g+c, K = 2P, scaled per G
+__global__ void k_split_x2(const double2* __restrict__ anl, int nproj, int ngw,
+                           const double* __restrict__ gmax, __half* __restrict__ X2,
+                           int nRT, int nKS, float* __restrict__ rscale) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  if (g >= ngw) return;
+  const int e = scale_exp(gmax[g]);
+  if (p == 0) {
+    rscale[2 * g] = ldexpf(1.f, e);
+    rscale[2 * g + 1] = ldexpf(1.f, e);
+  }
+  const double2 a = anl[(size_t)p * ngw + g];
+  const double re = ldexp(a.x, -e), im = ldexp(a.y, -e);
+  // X2[2g][2p]=re, X2[2g][2p+1]=-im, X2[2g+1][2p]=im, X2[2g+1][2p+1]=re
+  const double v[4] = {re, -im, im, re};
+  for (int q = 0; q < 4; ++q) {
+    const int r = 2 * g + (q >> 1), k = 2 * p + (q & 1);
+    __half hi, lo;
+    split2d(v[q], hi, lo);
+    X2[tc_index(0, r, k, nRT, nKS)] = hi;
+    X2[tc_index(1, r, k, nRT, nKS)] = lo;
+  }
+}
+
+// per-row max |x| of a complex FP64 block [nrows][ld] (first ncols complex)
+__global__ void k_rowmax_c64(const double2* __restrict__ x, int ld, int ncols,
+                             double* __restrict__ rmax) {
+  __shared__ double red[256];
+  const int n = blockIdx.x;
+  double m = 0.0;
+  for (int g = threadIdx.x; g < ncols; g += blockDim.x) {
+    const double2 a = x[(size_t)n * ld + g];
+    m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
+  }
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) rmax[n] = red[0];
+}
+
+// pieces of the interleaved real view of x[n][g] (K = 2*ncols), scaled per row
+__global__ void k_split_rows(const double2* __restrict__ x, int ld, int ncols,
+                             const double* __restrict__ rmax, __half* __restrict__ Y,
+                             int nRT, int nKS, float* __restrict__ rscale) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = blockIdx.y;
+  const int e = scale_exp(rmax[n]);
+  if (g == 0) rscale[n] = ldexpf(1.f, e);
+  if (g >= ncols) return;
+  const double2 a = x[(size_t)n * ld + g];
+  __half hi, lo;
+  split2d(ldexp(a.x, -e), hi, lo);
+  Y[tc_index(0, n, 2 * g, nRT, nKS)] = hi;
+  Y[tc_index(1, n, 2 * g, nRT, nKS)] = lo;
+  split2d(ldexp(a.y, -e), hi, lo);
+  Y[tc_index(0, n, 2 * g + 1, nRT, nKS)] = hi;
+  Y[tc_index(1, n, 2 * g + 1, nRT, nKS)] = lo;
+}
+
+// ------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+// bounded wait for the phase with parity `par` to complete; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par) {
+  for (long long it = 0; it < TC_SPIN; ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(su32(b)), "r"(par)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          su32(dst)),
+      "l"(src), "r"(bytes), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
+  // no-swizzle K-major canonical layout: LBO (K direction) 128 B, SBO (8-row
+  // groups) 256 B, descriptor version 1
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
+         ((uint64_t)(256 >> 4) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ uint32_t idesc_f16_f32(int m, int n) {
+  // D F32 (bit 4), A/B F16 (format 0), K-major, N>>3 at bit 17, M>>4 at 24
+  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc,
+                                        uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(da), "l"(db), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+      su32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t ta, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(ta));
+}
+__device__ __forceinline__ void tmem_st32(uint32_t ta, const uint32_t* r) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(ta),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
+      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
+      "r"(r[29]), "r"(r[30]), "r"(r[31]));
+}
+
+// epilogue modes
+enum { TC_OUT_PARTIAL = 0, TC_OUT_HPSI = 1 };
+
+struct TcArgs {
+  const __half* A;  // tile-canonical pieces, nRTa row tiles x nKS stages
+  const __half* B;  // tile-canonical pieces, nRTb row tiles x nKS stages
+  int nRTa, nRTb, nKS;
+  int M, N;         // valid rows of A / B
+  int ks_per_split; // K stages handled by one CTA (blockIdx.z)
+  const float* sA;  // per-row scales of A (length M)
+  const float* sB;  // per-row scales of B (length N)
+  double* out;      // PARTIAL: [split][N][M] doubles; HPSI: complex out, real view
+  int ldo;          // HPSI: leading dimension of out in complex elements
+  int* status;      // error word (1 = a bounded wait expired)
+};
+
+template <int MODE>
+__global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1 KB alignment of the stage ring
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + TC_STAGES * TC_STAGE_BYTES);
+  uint64_t* empty = full + TC_STAGES;
+  uint64_t* accfull = empty + TC_STAGES;
+  uint64_t* accempty = accfull + 2;
+  uint64_t* drain = accempty + 2;
+  uint32_t* tmem_slot = (uint32_t*)(drain + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mt = blockIdx.x, nt = blockIdx.y, z = blockIdx.z;
+  const int ks0 = z * args.ks_per_split;
+  const int nks = min(args.ks_per_split, args.nKS - ks0);
+  const int nchunks = (nks + TC_CHUNK - 1) / TC_CHUNK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&accfull[0], 1);
+    mbar_init(&accfull[1], 1);
+    mbar_init(&accempty[0], 128);
+    mbar_init(&accempty[1], 128);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     su32(tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tbase = *tmem_slot;
+  // tensor memory columns: [0,128) chunk buffer 0, [128,256) buffer 1,
+  // [256,384) running sum hi, [384,512) running sum lo
+  if (nks > 0) {
+    if (warp == 0 && lane == 0) {
+      // ---------------- producer
+      const size_t pieceA = (size_t)args.nRTa * args.nKS * (TC_BLOCK_BYTES / 2);
+      const size_t pieceB = (size_t)args.nRTb * args.nKS * (TC_BLOCK_BYTES / 2);
+      int issued = 0;
+      for (int i = 0; i < nks; ++i) {
+        const int s = i % TC_STAGES;
+        const uint32_t par = ((i / TC_STAGES) & 1) ^ 1;
+        if (i >= TC_STAGES && !mbar_wait(&empty[s], par)) {
+          *abort_flag = 1;
+          atomicExch(args.status, 1);
+          break;
+        }
+        if (*abort_flag) break;
+        unsigned char* st = smem + s * TC_STAGE_BYTES;
+        mbar_expect_tx(&full[s], TC_STAGE_BYTES);
+        const size_t oa = ((size_t)mt * args.nKS + ks0 + i) * (TC_BLOCK_BYTES / 2);
+        const size_t ob = ((size_t)nt * args.nKS + ks0 + i) * (TC_BLOCK_BYTES / 2);
+        bulk_g2s(st, args.A + oa, TC_BLOCK_BYTES, &full[s]);
+        bulk_g2s(st + TC_BLOCK_BYTES, args.A + pieceA + oa, TC_BLOCK_BYTES, &full[s]);
+        bulk_g2s(st + 2 * TC_BLOCK_BYTES, args.B + ob, TC_BLOCK_BYTES, &full[s]);
+        bulk_g2s(st + 3 * TC_BLOCK_BYTES, args.B + pieceB + ob, TC_BLOCK_BYTES, &full[s]);
+        issued = i + 1;
+      }
+      // no copy may still be landing in shared memory when the CTA retires
+      for (int i = max(0, issued - TC_STAGES); i < issued; ++i)
+        mbar_wait(&full[i % TC_STAGES], (i / TC_STAGES) & 1);
+    } else if (warp == 1 && lane == 0) {
+      // ---------------- MMA issuer
+      const uint32_t idesc = idesc_f16_f32(TC_M, TC_N);
+      int i = 0;
+      for (int c = 0; c < nchunks && !*abort_flag; ++c) {
+        const int b = c & 1;
+        if (c >= 2 && !mbar_wait(&accempty[b], ((c >> 1) - 1) & 1)) {
+          *abort_flag = 1;
+          atomicExch(args.status, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dcol = tbase + (uint32_t)(b * 128);
+        const int iend = min(nks, (c + 1) * TC_CHUNK);
+        bool first = true;
+        for (; i < iend; ++i) {
+          const int s = i % TC_STAGES;
+          if (!mbar_wait(&full[s], (i / TC_STAGES) & 1)) {
+            *abort_flag = 1;
+            atomicExch(args.status, 1);
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t st = su32(smem + s * TC_STAGE_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < 2; ++kk) {
+            const uint64_t a0 = sdesc(st + kk * 4096);
+            const uint64_t a1 = sdesc(st + TC_BLOCK_BYTES + kk * 4096);
+            const uint64_t b0 = sdesc(st + 2 * TC_BLOCK_BYTES + kk * 4096);
+            const uint64_t b1 = sdesc(st + 3 * TC_BLOCK_BYTES + kk * 4096);
+            mma_f16(dcol, a0, b0, idesc, first ? 0u : 1u);
+            first = false;
+            mma_f16(dcol, a0, b1, idesc, 1u);
+            mma_f16(dcol, a1, b0, idesc, 1u);
+          }
+          mma_commit(&empty[s]);  // frees the stage once these MMAs are done
+        }
+        mma_commit(&accfull[b]);
+        if (*abort_flag) break;
+      }
+      // every MMA of this thread has completed before tensor memory is freed
+      mma_commit(drain);
+      mbar_wait(drain, 0);
+    } else if (warp >= 2) {
+      // ---------------- epilogue: fold each chunk into the (hi, lo) sums
+      const int q = warp & 3;  // tensor memory lane quarter of this warp
+      const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+      for (int c = 0; c < nchunks; ++c) {
+        const int b = c & 1;
+        if (!mbar_wait(&accfull[b], (c >> 1) & 1)) {
+          *abort_flag = 1;
+          atomicExch(args.status, 1);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        for (int cb = 0; cb < 128; cb += 32) {
+          uint32_t p[32], h[32], l[32];
+          tmem_ld32(tbase + lane_off + b * 128 + cb, p);
+          if (c > 0) {
+            tmem_ld32(tbase + lane_off + 256 + cb, h);
+            tmem_ld32(tbase + lane_off + 384 + cb, l);
+          }
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float x = __uint_as_float(p[j]);
+            if (c == 0) {
+              h[j] = p[j];
+              l[j] = 0u;
+            } else {
+              const float a = __uint_as_float(h[j]);
+              const float s = a + x;
+              const float bb = s - a;
+              const float e = (a - (s - bb)) + (x - bb);
+              h[j] = __float_as_uint(s);
+              l[j] = __float_as_uint(__uint_as_float(l[j]) + e);
+            }
+          }
+          tmem_st32(tbase + lane_off + 256 + cb, h);
+          tmem_st32(tbase + lane_off + 384 + cb, l);
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        mbar_arrive(&accempty[b]);
+      }
+      // final write
+      if (!*abort_flag) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int m = mt * TC_M + q * 32 + lane;
+        const float sa = m < args.M ? args.sA[m] : 0.f;
+        for (int cb = 0; cb < 128; cb += 32) {
+          uint32_t h[32], l[32];
+          tmem_ld32(tbase + lane_off + 256 + cb, h);
+          tmem_ld32(tbase + lane_off + 384 + cb, l);
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+          if (m < args.M) {
+#pragma unroll
+            for (int j = 0; j < 32; ++j) {
+              const int n = nt * TC_N + cb + j;
+              if (n < args.N) {
+                const double v = ((double)__uint_as_float(h[j]) + (double)__uint_as_float(l[j])) *
+                                 (double)sa * (double)args.sB[n];
+                if (MODE == TC_OUT_PARTIAL)
+                  args.out[((size_t)z * args.N + n) * args.M + m] = v;
+                else
+                  args.out[(size_t)n * 2 * args.ldo + m] = v;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(512));
+}
+
+// ---------------------------------------------------------- reduce + split
+// fnl[n][p] = (D_p/Omega) * sum_z part[z][n][2p + c]; E_nl partials; the
+// per-state max |fnl| for the next split
+__global__ void k_tc_fnl_reduce(const double* __restrict__ part, int nsplit, int M, int nst,
+                                const double* __restrict__ wt, const double* __restrict__ occ,
+                                double2* __restrict__ fnl, double* __restrict__ enl_part) {
+  __shared__ double red[256];
+  const int P = M / 2;
+  const size_t total = (size_t)P * nst;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (i < total) {
+    const int n = (int)(i / P), p = (int)(i - (size_t)n * P);
+    double re = 0.0, im = 0.0;
+    for (int zz = 0; zz < nsplit; ++zz) {
+      const double* pz = part + ((size_t)zz * nst + n) * M;
+      re += pz[2 * p];
+      im += pz[2 * p + 1];
+    }
+    const double fac = wt[p];
+    e = (fac * (occ ? occ[n] : 0.0)) * (re * re + im * im);
+    fnl[i] = make_double2(fac * re, fac * im);
+  }
+  red[threadIdx.x] = e;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && enl_part) enl_part[blockIdx.x] = red[0];
+}
+
+// ------------------------------------------------------------- host side
+struct TcTables {
+  int P = 0, ngw = 0;
+  int x1_RT = 0, x1_KS = 0, x2_RT = 0, x2_KS = 0;
+  __half* X1 = nullptr;
+  __half* X2 = nullptr;
+  float* s1 = nullptr;  // per-row scales of X1 (2P)
+  float* s2 = nullptr;  // per-row scales of X2 (2ngw)
+  // per-H scratch
+  __half* Y = nullptr;  size_t Y_bytes = 0;
+  __half* F = nullptr;  size_t F_bytes = 0;
+  float* sY = nullptr;  size_t sY_bytes = 0;
+  float* sF = nullptr;  size_t sF_bytes = 0;
+  double* rmax = nullptr; size_t rmax_bytes = 0;
+  double* part = nullptr; size_t part_bytes = 0;
+  double2* fnl = nullptr; size_t fnl_bytes = 0;
+  int* status = nullptr;
+};
+
+static size_t pieces_bytes(int nRT, int nKS) { return 2ull * nRT * nKS * TC_BLOCK_BYTES; }
+
+static void tc_free(TcTables* t) {
+  if (!t) return;
+  void* bufs[] = {t->X1, t->X2, t->s1, t->s2, t->Y, t->F, t->sY, t->sF, t->rmax, t->part, t->fnl,
+                  t->status};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  delete t;
+}
+
+void tc_release(qbg_plan* p) {
+  tc_free((TcTables*)p->tc);
+  p->tc = nullptr;
+  p->tc_nst_cleared = 0;
+}
+
+qbg_status tc_build(qbg_plan* p, cudaStream_t st) {
+  tc_release(p);
+  if (p->nproj == 0 || p->ngw == 0) return QBG_OK;
+  TcTables* t = new TcTables;
+  p->tc = t;
+  t->P = p->nproj;
+  t->ngw = p->ngw;
+  t->x1_RT = (2 * t->P + TC_M - 1) / TC_M;
+  t->x1_KS = (2 * t->ngw + TC_KS - 1) / TC_KS;
+  t->x2_RT = (2 * t->ngw + TC_M - 1) / TC_M;
+  t->x2_KS = (2 * t->P + TC_KS - 1) / TC_KS;
+  const size_t b1 = pieces_bytes(t->x1_RT, t->x1_KS), b2 = pieces_bytes(t->x2_RT, t->x2_KS);
+  QBG_CUDA(cudaMalloc(&t->X1, b1));
+  QBG_CUDA(cudaMalloc(&t->X2, b2));
+  QBG_CUDA(cudaMemsetAsync(t->X1, 0, b1, st));
+  QBG_CUDA(cudaMemsetAsync(t->X2, 0, b2, st));
+  QBG_CUDA(cudaMalloc(&t->s1, sizeof(float) * 2 * t->P));
+  QBG_CUDA(cudaMalloc(&t->s2, sizeof(float) * 2 * (size_t)t->ngw));
+  QBG_CUDA(cudaMalloc(&t->status, sizeof(int)));
+  QBG_CUDA(cudaMemsetAsync(t->status, 0, sizeof(int), st));
+  double *pmax = nullptr, *gmax = nullptr;
+  QBG_CUDA(cudaMalloc(&pmax, sizeof(double) * t->P));
+  QBG_CUDA(cudaMalloc(&gmax, sizeof(double) * t->ngw));
+  k_anl_rowmax<<<t->P, 256, 0, st>>>(p->d_anl, t->P, t->ngw, pmax);
+  QBG_LAUNCHED(p);
+  k_anl_colmax<<<(t->ngw + 255) / 256, 256, 0, st>>>(p->d_anl, t->P, t->ngw, gmax);
+  QBG_LAUNCHED(p);
+  dim3 g((t->ngw + 255) / 256, t->P);
+  k_split_x1<<<g, 256, 0, st>>>(p->d_anl, t->P, t->ngw, pmax, t->X1, t->x1_RT, t->x1_KS, t->s1);
+  QBG_LAUNCHED(p);
+  k_split_x2<<<g, 256, 0, st>>>(p->d_anl, t->P, t->ngw, gmax, t->X2, t->x2_RT, t->x2_KS, t->s2);
+  QBG_LAUNCHED(p);
+  QBG_CUDA(cudaStreamSynchronize(st));
+  cudaFree(pmax);
+  cudaFree(gmax);
+  return QBG_OK;
+}
+
+static qbg_status tc_launch(qbg_plan* p, int mode, const TcArgs& a, int mt, int nt, int nsplit,
+                            cudaStream_t st) {
+  const size_t smem = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
+  if (mode == TC_OUT_PARTIAL) {
+    QBG_CUDA(cudaFuncSetAttribute(k_tc_gemm<TC_OUT_PARTIAL>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_tc_gemm<TC_OUT_PARTIAL><<<dim3(mt, nt, nsplit), TC_THREADS, smem, st>>>(a);
+  } else {
+    QBG_CUDA(cudaFuncSetAttribute(k_tc_gemm<TC_OUT_HPSI>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_tc_gemm<TC_OUT_HPSI><<<dim3(mt, nt, nsplit), TC_THREADS, smem, st>>>(a);
+  }
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+// out[n][g] = sum_p anl[p][g] fnl[n][p] with fnl = D/Omega <anl|psi>; psi and
+// out are FP64 [ld x nst]; enl partial sums into enl_part when given.
+qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
+                       const double* d_occ, double* enl_part, int* enl_blocks,
+                       cudaStream_t st) {
+  TcTables* t = (TcTables*)p->tc;
+  if (!t) QBG_TRY_TC(tc_build(p, st));
+  t = (TcTables*)p->tc;
+  if (!t) return QBG_OK;
+  const int P = t->P, ngw = t->ngw;
+  const int nRT = (nst + TC_N - 1) / TC_N;
+  // split psi
+  QBG_TRY_TC(ensure((void**)&t->Y, &t->Y_bytes, pieces_bytes(nRT, t->x1_KS)));
+  QBG_TRY_TC(ensure((void**)&t->sY, &t->sY_bytes, sizeof(float) * nRT * TC_N));
+  QBG_TRY_TC(ensure((void**)&t->rmax, &t->rmax_bytes, sizeof(double) * nRT * TC_N));
+  QBG_TRY_TC(ensure((void**)&t->F, &t->F_bytes, pieces_bytes(nRT, t->x2_KS)));
+  QBG_TRY_TC(ensure((void**)&t->sF, &t->sF_bytes, sizeof(float) * nRT * TC_N));
+  QBG_TRY_TC(ensure((void**)&t->fnl, &t->fnl_bytes, sizeof(double2) * (size_t)P * nst));
+  // the padding rows of the piece arrays stay zero: clear once per growth
+  if (t->Y_bytes && p->tc_nst_cleared < nst) {
+    QBG_CUDA(cudaMemsetAsync(t->Y, 0, t->Y_bytes, st));
+    QBG_CUDA(cudaMemsetAsync(t->F, 0, t->F_bytes, st));
+    p->tc_nst_cleared = nst;
+  }
+  {
+    PhaseTimer pt(p, PH_MISC, st);
+    k_rowmax_c64<<<nst, 256, 0, st>>>(psi, ld, ngw, t->rmax);
+    QBG_LAUNCHED(p);
+    k_split_rows<<<dim3((ngw + 255) / 256, nst), 256, 0, st>>>(psi, ld, ngw, t->rmax, t->Y, nRT,
+                                                              t->x1_KS, t->sY);
+    QBG_LAUNCHED(p);
+  }
+  // GEMM1 with split K
+  const int mt1 = t->x1_RT;
+  int nsplit = std::max(1, (3 * 152 + mt1 * nRT - 1) / (mt1 * nRT));
+  nsplit = std::min(nsplit, t->x1_KS);
+  const int ksp = (t->x1_KS + nsplit - 1) / nsplit;
+  nsplit = (t->x1_KS + ksp - 1) / ksp;
+  QBG_TRY_TC(ensure((void**)&t->part, &t->part_bytes, sizeof(double) * nsplit * nst * 2 * P));
+  TcArgs a1;
+  a1.A = t->X1;
+  a1.B = t->Y;
+  a1.nRTa = t->x1_RT;
+  a1.nRTb = nRT;
+  a1.nKS = t->x1_KS;
+  a1.M = 2 * P;
+  a1.N = nst;
+  a1.ks_per_split = ksp;
+  a1.sA = t->s1;
+  a1.sB = t->sY;
+  a1.out = t->part;
+  a1.ldo = 0;
+  a1.status = t->status;
+  {
+    PhaseTimer pt(p, PH_FNL_GEMM, st);
+    QBG_TRY_TC(tc_launch(p, TC_OUT_PARTIAL, a1, mt1, nRT, nsplit, st));
+  }
+  const size_t total = (size_t)P * nst;
+  const int rb = (int)((total + 255) / 256);
+  *enl_blocks = rb;
+  {
+    PhaseTimer pt(p, PH_FNL_REDUCE, st);
+    k_tc_fnl_reduce<<<rb, 256, 0, st>>>(t->part, nsplit, 2 * P, nst, p->d_pwt, d_occ, t->fnl,
+                                        enl_part);
+    QBG_LAUNCHED(p);
+    k_rowmax_c64<<<nst, 256, 0, st>>>(t->fnl, P, P, t->rmax);
+    QBG_LAUNCHED(p);
+    k_split_rows<<<dim3((P + 255) / 256, nst), 256, 0, st>>>(t->fnl, P, P, t->rmax, t->F, nRT,
+                                                            t->x2_KS, t->sF);
+    QBG_LAUNCHED(p);
+  }
+  // GEMM2 writes the NL part of H psi
+  TcArgs a2;
+  a2.A = t->X2;
+  a2.B = t->F;
+  a2.nRTa = t->x2_RT;
+  a2.nRTb = nRT;
+  a2.nKS = t->x2_KS;
+  a2.M = 2 * ngw;
+  a2.N = nst;
+  a2.ks_per_split = t->x2_KS;
+  a2.sA = t->s2;
+  a2.sB = t->sF;
+  a2.out = (double*)out;
+  a2.ldo = ld;
+  a2.status = t->status;
+  {
+    PhaseTimer pt(p, PH_ENL_HPSI, st);
+    QBG_TRY_TC(tc_launch(p, TC_OUT_HPSI, a2, t->x2_RT, nRT, 1, st));
+  }
+  return QBG_OK;
+}
+
+qbg_status tc_check_status(qbg_plan* p) {
+  TcTables* t = (TcTables*)p->tc;
+  if (!t) return QBG_OK;
+  int s = 0;
+  QBG_CUDA(cudaMemcpy(&s, t->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (s) {
+    set_error("tensor-core GEMM: a bounded wait expired (status %d)", s);
+    cudaMemset(t->status, 0, sizeof(int));
+    return QBG_ERR_TIMEOUT;
+  }
+  return QBG_OK;
+}
+
+}  // namespace qbg

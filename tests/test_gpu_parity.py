@@ -200,6 +200,30 @@ def test_etrs_time_dependent_vector_potential(cuda):
     assert rel_err(p.cpu().numpy(), ref.T) < 1e-10
 
 
+@pytest.mark.parametrize("name", ["t12", "c1"])
+def test_hpsi_mixed_vs_oracle(cuda, name):
+    """FP32 transforms + tensor-core projector GEMMs (2-piece FP16 split),
+    FP64 kinetic term and FP64 in/out: <= 2e-6 relative to the FP64 oracle."""
+    cell, b, H, oft, oh, psi = setup(name, prec="mixed")
+    occ = synth.occupations(cell)
+    torch = _torch()
+    out = torch.zeros_like(dev(psi))
+    enl = H.hpsi(dev(psi), out, occ, want_enl=True)
+    ref, enl_ref = oh.hpsi(psi.T, occ, nthreads=NT)
+    err = rel_err(out.cpu().numpy(), ref.T)
+    assert err < 2e-6, err
+    assert abs(enl - enl_ref) <= 2e-6 * abs(enl_ref)
+    # the nonlocal part alone through the tensor cores
+    parts, _ = oh.parts(psi.T, occ, nthreads=NT)
+    Hloc = Q.Hamiltonian(b, *cell.grid, precision="mixed")
+    Hloc.set_vlocal(np.zeros(oft.n012))
+    Hloc.set_nonlocal(synth.species(cell))
+    out2 = torch.zeros_like(out)
+    Hloc.hpsi(dev(psi), out2, occ)
+    nl_ref = parts[0].T + parts[1].T  # nonlocal + kinetic (v = 0)
+    assert rel_err(out2.cpu().numpy(), nl_ref) < 2e-6
+
+
 def test_etrs_mixed_error_vs_fp64_oracle(cuda):
     cell, b, H, oft, oh, psi = setup("t12", prec="mixed")
     occ = synth.occupations(cell)
