@@ -49,7 +49,7 @@ constexpr int TC_CHUNK = 8;        // stages per tensor-memory chunk (K = 256)
 constexpr int TC_BLOCK_BYTES = TC_M * TC_KS * 2;   // 8 KB per piece per stage
 constexpr int TC_STAGE_BYTES = 4 * TC_BLOCK_BYTES; // A0 A1 B0 B1
 constexpr int TC_THREADS = 192;
-constexpr long long TC_SPIN = 1LL << 22;
+constexpr int TC_SPIN = 1 << 21;   // polls per bounded wait (~0.2 s with backoff)
 
 // byte offset of element (r, k) inside one 128x32 block image
 __host__ __device__ __forceinline__ int tc_canon(int r, int k) {
@@ -215,16 +215,19 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
 }
 // bounded wait for the phase with parity `par` to complete; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par) {
-  for (long long it = 0; it < TC_SPIN; ++it) {
+// or when another CTA has already raised the grid-wide error word
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, const int* gstatus) {
+  for (int it = 0; it < TC_SPIN; ++it) {
     uint32_t ok;
     asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
         "selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
         : "r"(su32(b)), "r"(par)
         : "memory");
     if (ok) return true;
+    if (it > 64) __nanosleep(64);
+    if ((it & 4095) == 4095 && *(volatile const int*)gstatus) return false;
   }
   return false;
 }
@@ -311,7 +314,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mt = blockIdx.x, nt = blockIdx.y, z = blockIdx.z;
   const int ks0 = z * args.ks_per_split;
-  const int nks = min(args.ks_per_split, args.nKS - ks0);
+  // a CTA that starts after another one failed does no work
+  const int nks = *(volatile const int*)args.status ? 0 : min(args.ks_per_split, args.nKS - ks0);
   const int nchunks = (nks + TC_CHUNK - 1) / TC_CHUNK;
 
   if (threadIdx.x == 0) {
@@ -347,7 +351,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       for (int i = 0; i < nks; ++i) {
         const int s = i % TC_STAGES;
         const uint32_t par = ((i / TC_STAGES) & 1) ^ 1;
-        if (i >= TC_STAGES && !mbar_wait(&empty[s], par)) {
+        if (i >= TC_STAGES && !mbar_wait(&empty[s], par, args.status)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
           break;
@@ -365,14 +369,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       }
       // no copy may still be landing in shared memory when the CTA retires
       for (int i = max(0, issued - TC_STAGES); i < issued; ++i)
-        mbar_wait(&full[i % TC_STAGES], (i / TC_STAGES) & 1);
+        mbar_wait(&full[i % TC_STAGES], (i / TC_STAGES) & 1, args.status);
     } else if (warp == 1 && lane == 0) {
       // ---------------- MMA issuer
       const uint32_t idesc = idesc_f16_f32(TC_M, TC_N);
       int i = 0;
       for (int c = 0; c < nchunks && !*abort_flag; ++c) {
         const int b = c & 1;
-        if (c >= 2 && !mbar_wait(&accempty[b], ((c >> 1) - 1) & 1)) {
+        if (c >= 2 && !mbar_wait(&accempty[b], ((c >> 1) - 1) & 1, args.status)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
           break;
@@ -383,7 +387,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
         bool first = true;
         for (; i < iend; ++i) {
           const int s = i % TC_STAGES;
-          if (!mbar_wait(&full[s], (i / TC_STAGES) & 1)) {
+          if (!mbar_wait(&full[s], (i / TC_STAGES) & 1, args.status)) {
             *abort_flag = 1;
             atomicExch(args.status, 1);
             break;
@@ -408,14 +412,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       }
       // every MMA of this thread has completed before tensor memory is freed
       mma_commit(drain);
-      mbar_wait(drain, 0);
+      mbar_wait(drain, 0, args.status);
     } else if (warp >= 2) {
       // ---------------- epilogue: fold each chunk into the (hi, lo) sums
       const int q = warp & 3;  // tensor memory lane quarter of this warp
       const uint32_t lane_off = (uint32_t)(q * 32) << 16;
       for (int c = 0; c < nchunks; ++c) {
         const int b = c & 1;
-        if (!mbar_wait(&accfull[b], (c >> 1) & 1)) {
+        if (!mbar_wait(&accfull[b], (c >> 1) & 1, args.status)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
           break;
