@@ -48,9 +48,12 @@ typedef enum {
 } qbg_status;
 
 enum {
-  QBG_PREC_FP64 = 0,  /* plain form: FP64 storage and FP64 arithmetic */
-  QBG_PREC_MIXED = 1  /* FP32 transforms, tensor-core projector GEMMs,
-                         FP64 Taylor accumulation and reductions */
+  QBG_PREC_FP64 = 0,        /* plain form: FP64 storage and FP64 arithmetic */
+  QBG_PREC_MIXED = 1,       /* FP32 transforms, tensor-core projector GEMMs
+                               (2-piece FP16 split), FP64 kinetic term, FP64
+                               wavefunctions, Taylor sums and reductions */
+  QBG_PREC_MIXED_FFT64 = 2, /* as MIXED but FP64 transforms */
+  QBG_PREC_MIXED_NL64 = 3   /* as MIXED but FP64 projector GEMMs */
 };
 
 typedef struct qbg_plan qbg_plan;

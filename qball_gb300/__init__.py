@@ -30,6 +30,10 @@ LIBPATH = os.path.join(HERE, "libqbg.so")
 
 QBG_PREC_FP64 = 0
 QBG_PREC_MIXED = 1
+QBG_PREC_MIXED_FFT64 = 2
+QBG_PREC_MIXED_NL64 = 3
+PRECISIONS = {"fp64": QBG_PREC_FP64, "mixed": QBG_PREC_MIXED,
+              "mixed_fft64": QBG_PREC_MIXED_FFT64, "mixed_nl64": QBG_PREC_MIXED_NL64}
 _STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "unsupported",
            4: "CUDA error", 5: "timeout", 6: "diverged", 7: "bad state"}
 
@@ -161,7 +165,9 @@ class FourierTransform:
         self.shape = (int(np0), int(np1), int(np2))
         self.n012 = int(np0) * int(np1) * int(np2)
         self.precision = precision
-        prec = QBG_PREC_MIXED if precision == "mixed" else QBG_PREC_FP64
+        if precision not in PRECISIONS:
+            raise QbgError(f"unknown precision {precision!r}; one of {sorted(PRECISIONS)}")
+        prec = PRECISIONS[precision]
         d = _BasisDesc(basis.ngw, basis.nrods, _np_ptr(basis.rod_h), _np_ptr(basis.rod_k),
                        _np_ptr(basis.rod_lmin), _np_ptr(basis.rod_size), _np_ptr(basis.kpgx),
                        basis.omega)
@@ -169,7 +175,7 @@ class FourierTransform:
         _check(lib().qbg_plan_create(ctypes.byref(d), int(np0), int(np1), int(np2), prec,
                                      ctypes.byref(h)), "qbg_plan_create")
         self.h = h
-        self.chunk = 16 if prec == QBG_PREC_MIXED else 8  # the plan's default
+        self.chunk = 16 if prec in (QBG_PREC_MIXED, QBG_PREC_MIXED_NL64) else 8  # plan default
 
     def close(self):
         if getattr(self, "h", None):

@@ -62,6 +62,7 @@ def main():
     ap.add_argument("--dt", type=float, default=0.05)
     ap.add_argument("--forms", default="fp64,mixed")
     ap.add_argument("--out", default="")
+    ap.add_argument("--ref", default="", help="npz of an earlier run: reuse its fp64 d(t)")
     args = ap.parse_args()
     kw = {"nst": args.nst} if args.nst else {}
     cell = synth.make_cell(args.config, **kw)
@@ -72,6 +73,10 @@ def main():
     res = {}
     for form in args.forms.split(","):
         res[form] = run_form(form, cell, basis, psi0, occ, A, args.dt, args.steps)
+    if args.ref:
+        z = np.load(args.ref)
+        ref = {"d": z["fp64_d"][:args.steps + 1], "J": z["fp64_J"][:args.steps + 1], "psi": None}
+        res.setdefault("fp64", ref)
     ref = res["fp64"]
     dref = ref["d"]
     scale_z = np.abs(dref[:, 2]).max()
@@ -82,11 +87,13 @@ def main():
         dd = r["d"] - dref
         rel_z = float(np.abs(dd[:, 2]).max() / scale_z)
         rel_n = float(np.linalg.norm(dd, axis=1).max() / scale_n)
-        pd = float(((r["psi"] - ref["psi"]).abs().pow(2).sum().sqrt()
-                    / ref["psi"].abs().pow(2).sum().sqrt()).item())
+        pd = (float(((r["psi"] - ref["psi"]).abs().pow(2).sum().sqrt()
+                     / ref["psi"].abs().pow(2).sum().sqrt()).item())
+              if r["psi"] is not None and ref["psi"] is not None else None)
         report["forms"][form] = {"dipole_rel_err_z": rel_z, "dipole_rel_err_norm": rel_n,
-                                 "psi_rel_err_final": pd, "seconds": r["seconds"],
-                                 "steps_per_s": args.steps / r["seconds"]}
+                                 "psi_rel_err_final": pd, "seconds": r.get("seconds"),
+                                 "steps_per_s": (args.steps / r["seconds"]) if r.get("seconds")
+                                 else None}
     print(json.dumps(report), flush=True)
     if args.out:
         np.savez(args.out, **{f"{k}_d": v["d"] for k, v in res.items()},

@@ -124,8 +124,21 @@ static qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* ou
     }
     return local_hpsi<double>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
   }
-  if (nl) QBG_TRY(tc_nl_apply(p, psi, ld, out, nst, d_occ, enl_part, enl_blocks, st));
+  if (nl) {
+    if (p->prec == QBG_PREC_MIXED_NL64) {
+      QBG_TRY(nl_apply<double>(p, psi, ld, out, nst, d_occ, enl_part, st));
+      *enl_blocks = nl_reduce_blocks(p, nst);
+    } else {
+      QBG_TRY(tc_nl_apply(p, psi, ld, out, nst, d_occ, enl_part, enl_blocks, st));
+    }
+  }
+  if (p->prec == QBG_PREC_MIXED_FFT64)
+    return local_hpsi<double>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
   return local_hpsi<float>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
+}
+
+static bool uses_tc(const qbg_plan* p) {
+  return p->prec == QBG_PREC_MIXED || p->prec == QBG_PREC_MIXED_FFT64;
 }
 
 static qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, const char* who) {
@@ -246,7 +259,7 @@ qbg_status qbg_hpsi(qbg_plan* p, const double* psi, int ld, double* hpsi, int ns
   int nb = 0;
   QBG_TRY(hpsi_core(p, (const double2*)psi, ld, (double2*)hpsi, nst, d_occ,
                     enl ? p->d_red : nullptr, &nb, nullptr, 0, zero, st));
-  if (p->prec == QBG_PREC_MIXED) QBG_TRY(tc_check_status(p));
+  if (uses_tc(p)) QBG_TRY(tc_check_status(p));
   if (enl) {
     *enl = 0.0;
     if (nb > 0) {
@@ -278,7 +291,8 @@ static qbg_status sum_device(qbg_plan* p, const double* x, long long n, double* 
 
 static qbg_status density_any(qbg_plan* p, const double2* psi, int ld, int nst,
                               const double* d_w, double* rho, cudaStream_t st) {
-  if (p->prec == QBG_PREC_FP64) return density<double>(p, psi, ld, nst, d_w, rho, st);
+  if (p->prec == QBG_PREC_FP64 || p->prec == QBG_PREC_MIXED_FFT64)
+    return density<double>(p, psi, ld, nst, d_w, rho, st);
   return density<float>(p, psi, ld, nst, d_w, rho, st);
 }
 
@@ -396,7 +410,7 @@ qbg_status qbg_etrs_step(qbg_plan* p, double* psi_, int ld, int nst, const doubl
   }
   if (A_tdt) QBG_TRY(qbg_set_vector_potential(p, A_tdt));
   QBG_TRY(exponential(p, psi, ld, nst, d_occ, dt1, st));
-  if (p->prec == QBG_PREC_MIXED && p->check_every_step) QBG_TRY(tc_check_status(p));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
   return QBG_OK;
 }
 

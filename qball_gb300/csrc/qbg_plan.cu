@@ -380,7 +380,7 @@ qbg_status qbg_plan_create(const qbg_basis_desc* bd, int np0, int np1, int np2,
                            int precision, qbg_plan** out) {
   if (!bd || !out || bd->ngw < 0 || bd->nrods < 0 || np0 <= 0 || np1 <= 0 || np2 <= 0 ||
       (bd->ngw > 0 && (!bd->rod_h || !bd->rod_k || !bd->rod_lmin || !bd->rod_size || !bd->kpgx)) ||
-      (precision != QBG_PREC_FP64 && precision != QBG_PREC_MIXED) || !(bd->omega > 0.0)) {
+      precision < QBG_PREC_FP64 || precision > QBG_PREC_MIXED_NL64 || !(bd->omega > 0.0)) {
     set_error("qbg_plan_create: invalid argument");
     return QBG_ERR_INVALID;
   }
@@ -491,7 +491,7 @@ qbg_status qbg_plan_create(const qbg_basis_desc* bd, int np0, int np1, int np2,
     qbg_plan_destroy(p);
     return st;
   }
-  p->chunk = precision == QBG_PREC_FP64 ? 8 : 16;
+  p->chunk = (precision == QBG_PREC_FP64 || precision == QBG_PREC_MIXED_FFT64) ? 8 : 16;
   *out = p;
   return QBG_OK;
 }
