@@ -101,6 +101,23 @@ qbg_status qbg_plan_set_chunk(qbg_plan* plan, int states_per_chunk);
  * nbatch states: c [ldc x nbatch] complex, f [N x nbatch] complex (FP64). */
 qbg_status qbg_backward(qbg_plan* plan, const double* c, int ldc, double* f,
                         int nbatch, void* stream);
+/* qbg_backward for callers that cannot allocate device memory at call time
+ * (for example code being captured into a CUDA graph, where cudaMalloc
+ * cannot be recorded, or a host application whose device memory is owned
+ * by its own pool).  No counterpart in the reference.  Same arguments and
+ * results as qbg_backward, but its scratch comes from one static 32 MiB
+ * device array that the library holds on every GPU until exit instead of a
+ * plan buffer, and it calls no cudaMalloc/cudaFree.  Limit: one state's
+ * intermediates, 16*np2*(nrods + nband*np0) bytes with nband =
+ * 2*(max|k|+1), must fit in 32 MiB, else QBG_ERR_INVALID.  The first call
+ * on a device resolves the array's device address (make that first call
+ * before any stream capture).  Calls share the array: two calls whose
+ * kernels overlap on the GPU race, so serialise them (one stream).  The
+ * array needs no clearing (every element read is first written by the same
+ * call). */
+qbg_status qbg_backward_noalloc(qbg_plan* plan, const double* c, int ldc,
+                                double* f, int nbatch, void* stream);
+
 /* FourierTransform::forward(f, c) (FourierTransform.cc:542), batched; like
  * the reference, f is overwritten (used as scratch). */
 qbg_status qbg_forward(qbg_plan* plan, double* f, double* c, int ldc,

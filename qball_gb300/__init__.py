@@ -51,6 +51,7 @@ ABI = {
     "qbg_plan_destroy": [_P],
     "qbg_plan_set_chunk": [_P, _I],
     "qbg_backward": [_P, _P, _I, _P, _I, _P],
+    "qbg_backward_noalloc": [_P, _P, _I, _P, _I, _P],
     "qbg_forward": [_P, _P, _P, _I, _I, _P],
     "qbg_set_vlocal": [_P, _P],
     "qbg_set_nonlocal": [_P, _I, _P, _P, _P, _P, _P],

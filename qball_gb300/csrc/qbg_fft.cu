@@ -494,6 +494,54 @@ qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst, const double
   return QBG_OK;
 }
 
+// Backward transform with caller-provided scratch (Z for chunk*n2*nrods,
+// Y for chunk*n2*nband*n0 complex elements of type T); allocates nothing.
+template <typename T, bool BX, bool BY, bool BZ>
+static qbg_status backward_scratch_(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,
+                                    cplx<T>* Z, cplx<T>* Y, int chunk, cudaStream_t st) {
+  const FFTLen<T> dz = p->len[2].view<T>(), dx = p->len[0].view<T>(), dy = p->len[1].view<T>();
+  const size_t smz = smem_bytes<T>(dz.n), smx = smem_bytes<T>(dx.n), smy = smem_bytes<T>(dy.n);
+  QBG_CUDA(prep(k_z_bwd<T, BZ>, smz));
+  QBG_CUDA(prep(k_x_bwd<T, BX>, smx));
+  QBG_CUDA((prep(k_y<T, Y_BWD_STORE, BY>, smy)));
+  for (int s0 = 0; s0 < nb; s0 += chunk) {
+    const int ns = std::min(chunk, nb - s0);
+    k_z_bwd<T, BZ><<<dim3((p->nrods + kTile - 1) / kTile, ns), kThreads, smz, st>>>(
+        c + (size_t)s0 * ldc, ldc, Z, p->d_rods, p->nrods, dz);
+    QBG_LAUNCHED(p);
+    k_x_bwd<T, BX><<<dim3(p->np2 * ((p->nband + kTile - 1) / kTile), ns), kThreads, smx, st>>>(
+        Z, Y, p->nrods, p->nband, p->np2, p->d_row_ptr, p->d_row_rod, p->d_row_x, dx);
+    QBG_LAUNCHED(p);
+    k_y<T, Y_BWD_STORE, BY><<<dim3(p->np2 * ((p->np0 + kTile - 1) / kTile), ns), kThreads, smy,
+                              st>>>(Y, p->nband, p->np0, p->np2, p->d_band_y, nullptr,
+                                    f + (size_t)s0 * p->N, nullptr, ns, nullptr, 0, dy);
+    QBG_LAUNCHED(p);
+  }
+  return QBG_OK;
+}
+
+template <typename T>
+qbg_status backward_scratch(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,
+                            void* Z, void* Y, int chunk, cudaStream_t st) {
+  const bool bx = big_prime(p->len[0]), by = big_prime(p->len[1]), bz = big_prime(p->len[2]);
+  cplx<T>* z = (cplx<T>*)Z;
+  cplx<T>* y = (cplx<T>*)Y;
+  // the three lengths are dispatched independently
+  if (bx) {
+    if (by) return bz ? backward_scratch_<T, true, true, true>(p, c, ldc, f, nb, z, y, chunk, st)
+                      : backward_scratch_<T, true, true, false>(p, c, ldc, f, nb, z, y, chunk, st);
+    return bz ? backward_scratch_<T, true, false, true>(p, c, ldc, f, nb, z, y, chunk, st)
+              : backward_scratch_<T, true, false, false>(p, c, ldc, f, nb, z, y, chunk, st);
+  }
+  if (by) return bz ? backward_scratch_<T, false, true, true>(p, c, ldc, f, nb, z, y, chunk, st)
+                    : backward_scratch_<T, false, true, false>(p, c, ldc, f, nb, z, y, chunk, st);
+  return bz ? backward_scratch_<T, false, false, true>(p, c, ldc, f, nb, z, y, chunk, st)
+            : backward_scratch_<T, false, false, false>(p, c, ldc, f, nb, z, y, chunk, st);
+}
+
+template qbg_status backward_scratch<double>(qbg_plan*, const double2*, int, double2*, int, void*,
+                                             void*, int, cudaStream_t);
+
 template qbg_status local_hpsi<double>(qbg_plan*, const double2*, int, double2*, int, bool,
                                        double2*, int, double2, cudaStream_t);
 template qbg_status local_hpsi<float>(qbg_plan*, const double2*, int, double2*, int, bool,

@@ -174,6 +174,9 @@ qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb,
 template <typename T>
 qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst,
                    const double* d_w, double* rho, cudaStream_t st);
+template <typename T>
+qbg_status backward_scratch(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,
+                            void* Z, void* Y, int chunk, cudaStream_t st);
 
 // nonlocal (qbg_nl.cu)
 qbg_status nl_build(qbg_plan* p, cudaStream_t st);
