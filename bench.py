@@ -1,6 +1,13 @@
 #!/usr/bin/env python3
 """ETRS steps/s on the 216-atom cell: mixed precision vs the plain FP64 form.
 
+`value` times the precision form given by --form (default mixed_fft64: FP64
+transforms, projector GEMMs on the tensor cores) -- the fastest form whose
+200-step dipole stays within 1e-8 (relative) of the plain FP64 form
+(profiles/accuracy.json, produced by python -m qball_gb300.accuracy).  The
+FP32-transform form (--also, default mixed) and the plain FP64 form are timed
+beside it under `other_forms`.
+
 One "step" is one ETRS step of ExponentialWavefunctionStepper (preupdate +
 update: three 4th-order Taylor exponentials = 12 H|psi> applications, plus
 the density of the predicted state) over all 432 states of the synthetic
@@ -50,6 +57,12 @@ def parse():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--form", default="mixed_fft64",
+                    help="precision form timed for `value` (the fastest form whose 200-step "
+                         "dipole error is within 1e-8 of the FP64 form)")
+    ap.add_argument("--also", default="mixed", help="a second form timed beside it")
+    ap.add_argument("--also-steps", type=int, default=3)
+    ap.add_argument("--also-warmup", type=int, default=3)
     return ap.parse_args()
 
 
@@ -139,7 +152,6 @@ class Clocks:
 
 # ------------------------------------------------------------ system
 def make_system(cfg, precision, psi_np=None, chunk=0):
-    import torch
     import qball_gb300 as Q
     from qball_gb300 import synth
     cell = synth.make_cell(cfg)
@@ -188,28 +200,65 @@ def time_etrs(H, p, occ, dt, A, steps, warmup, stream):
 
 
 # ------------------------------------------------------------ roofline
-def phase_units(H, cell, basis, nst):
-    """Algorithmic bytes (HBM) or flops per launch of each phase."""
-    P = H.nproj if hasattr(H, "nproj") else None
+def phase_model(H, cell, basis, nst):
+    """Per-launch algorithmic work of each phase: (kind, amount) where kind is
+    'flop' (5 n log2 n per 1-D transform, the reference's own FFT model in
+    testFourierTransform.cc; 2*M*N*K per real GEMM product on the tensor
+    pipe) or 'byte' (compulsory HBM bytes)."""
     n0, n1, n2 = cell.grid
     ngw, nrods = basis.ngw, basis.nrods
     nband = 2 * (max(abs(basis.idxmin[1]), abs(basis.idxmax[1])) + 1)
-    cs = 8 if H.precision == "mixed" else 16      # complex element bytes
-    rs = 4 if H.precision == "mixed" else 8       # real element bytes
-    chunk = H.chunk
-    return dict(
-        fnl_gemm=("flop", 8.0 * nproj_of(cell) * ngw * nst),
-        enl_hpsi=("flop", 8.0 * nproj_of(cell) * ngw * nst),
-        ft_z_bwd=("byte", chunk * (ngw * cs + n2 * nrods * cs)),
-        ft_x_bwd=("byte", chunk * n2 * (nrods * cs + nband * n0 * cs)),
-        ft_y_vloc=("byte", chunk * n2 * (2 * nband * n0 * cs) + n0 * n1 * n2 * rs),
-        ft_x_fwd=("byte", chunk * n2 * (nrods * cs + nband * n0 * cs)),
-        ft_z_fwd=("byte", chunk * (n2 * nrods * cs + 3 * ngw * cs + 2 * ngw * 16)),
-    )
+    P = nproj_of(cell)
+    ch = H.chunk
+    f = lambda n: 5.0 * n * np.log2(n)
+    fft64 = H.precision in ("fp64", "mixed_fft64")
+    tc = H.precision in ("mixed", "mixed_fft64")
+    m = {}
+    m["ft_z_bwd"] = ("flop", ch * nrods * f(n2))
+    m["ft_x_bwd"] = ("flop", ch * n2 * nband * f(n0))
+    m["ft_y_vloc"] = ("flop", ch * n2 * n0 * 2 * f(n1))
+    m["ft_x_fwd"] = m["ft_x_bwd"]
+    m["ft_z_fwd"] = m["ft_z_bwd"]
+    gemm = 8.0 * P * ngw * nst          # one complex GEMM
+    m["fnl_gemm"] = ("flop", 3 * gemm if tc else gemm)   # 3 split products on the tensor pipe
+    m["enl_hpsi"] = ("flop", 3 * gemm if tc else gemm)
+    bounds = {}
+    for k in m:
+        if k.startswith("ft_"):
+            bounds[k] = ("fp64", 1.007) if fft64 else ("fp32", 72.2)
+        else:
+            bounds[k] = ("tensor", None) if tc else ("fp64", 1.007)
+    return m, bounds
 
 
 def nproj_of(cell):
     return cell.natoms * (cell.lmax + 1) ** 2
+
+
+def roofline_of(H, cell, basis, prof, peaks):
+    model, bounds = phase_model(H, cell, basis, cell.nst)
+    dom = max(model, key=lambda k: prof.get(k, (0, 0))[0])
+    tot_ms, nl = prof[dom]
+    per_launch_s = tot_ms / 1000.0 / max(nl, 1)
+    kind, amount = model[dom]
+    bound, peak = bounds[dom]
+    if bound == "tensor":
+        peak = float(peaks.get("bf16_tflops", 1917.4))
+    achieved = amount / per_launch_s / 1e12
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(HERE, "profiles", "traffic.json")))
+        key = f"{H.precision}:{dom}"
+        if key in tr:
+            traffic = tr[key]["bytes_per_launch"]
+    except (OSError, ValueError):
+        pass
+    return {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+            "per_launch_ms": per_launch_s * 1e3,
+            "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 kind::f16 runs at the same "
+                            "rate)" if bound == "tensor" else "profiles/peaks_gb300.txt"),
+            "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]}}
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -273,13 +322,26 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def accuracy_table():
+    try:
+        a = json.load(open(os.path.join(HERE, "profiles", "accuracy.json")))
+        return a.get("c2_216atoms_16states", {})
+    except (OSError, ValueError):
+        return {}
+
+
 def run_ours(args, rank, world, local):
     import torch
-    import qball_gb300 as Q
     from qball_gb300 import synth
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
-    cell, basis, H, psi = make_system(args.config, "mixed", chunk=args.chunk)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    acc = accuracy_table()
+    cell, basis, H, psi = make_system(args.config, args.form, chunk=args.chunk)
     occ = synth.occupations(cell)
     A = synth.kick()
     H.set_vector_potential(A)
@@ -299,36 +361,7 @@ def run_ours(args, rank, world, local):
     H.hpsi(p, hp, occ, stream=stream)
     prof = H.profile_read()
     H.profile(False)
-    units = phase_units(H, cell, basis, cell.nst)
-    dom = max(units, key=lambda k: prof[k][0])
-    tot_ms, nl = prof[dom]
-    kind, amount = units[dom]
-    per_launch_s = tot_ms / 1000.0 / max(nl, 1)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        pass
-    if kind == "flop":
-        bound, unit_r = "fp32_fma" if True else "tensor", "TFLOP/s"
-        achieved = amount / per_launch_s / 1e12
-        peak = 72.2  # measured FFMA peak on this GB300 (profiles/peaks_gb300.txt)
-    else:
-        bound, unit_r = "hbm", "GB/s"
-        per_launch_amount = amount
-        achieved = per_launch_amount / per_launch_s / 1e9
-        peak = float(peaks.get("hbm_gbs", 6800.0))
-    traffic = None
-    try:
-        tr = json.load(open(os.path.join(HERE, "profiles", "traffic.json")))
-        if dom in tr and tr[dom].get("config") == args.config:
-            traffic = tr[dom]["bytes_per_launch"]
-    except (OSError, ValueError):
-        pass
-    roofline = {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
-                "unit": unit_r, "frac": achieved / peak, "traffic": traffic,
-                "per_launch_ms": per_launch_s * 1e3,
-                "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]}}
+    roofline = roofline_of(H, cell, basis, prof, peaks)
 
     # end to end through the public API with host buffers
     e2e = None
@@ -351,40 +384,52 @@ def run_ours(args, rank, world, local):
         e1.record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-        e2e_ms = e0.elapsed_time(e1)
-        e2e_ms = allreduce_max(e2e_ms, world)
+        e2e_ms = allreduce_max(e0.elapsed_time(e1), world)
         e2e = {"value": world * args.e2e_steps / (e2e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes + 24,
                "steps": args.e2e_steps, "wall_s": wall, "J_last": list(map(float, J))}
         del h_in, h_out
+    del H
+    torch.cuda.empty_cache()
 
-    # plain FP64 form on the same cell
-    fp64 = None
-    if not args.skip_fp64:
-        del H
+    # the other forms on the same cell and states
+    others = {}
+    for form, steps, warm in ((args.also, args.also_steps, args.also_warmup),
+                              ("fp64", args.fp64_steps, args.fp64_warmup)):
+        if not form or (form == "fp64" and args.skip_fp64):
+            continue
+        _, _, H2, _ = make_system(args.config, form, psi_np=psi)
+        H2.set_vector_potential(A)
+        p2 = psi.clone()
+        ms2, _ = time_etrs(H2, p2, occ, args.dt, A, steps, warm, stream)
+        ms2 = allreduce_max(ms2, world)
+        H2.profile(True)
+        H2.hpsi(p2, hp, occ, stream=stream)
+        pr2 = H2.profile_read()
+        H2.profile(False)
+        others[form] = {"value": world * steps / (ms2 / 1000.0), "unit": UNIT, "steps": steps,
+                        "warmup": warm, "dipole_rel_err_200_steps": acc.get(form),
+                        "phases_ms_per_H": {k: round(v[0], 3) for k, v in pr2.items() if v[1]}}
+        del H2, p2
         torch.cuda.empty_cache()
-        _, _, H64, _ = make_system(args.config, "fp64", psi_np=psi)
-        H64.set_vector_potential(A)
-        p64 = psi.clone()
-        ms64, _ = time_etrs(H64, p64, occ, args.dt, A, args.fp64_steps, args.fp64_warmup, stream)
-        ms64 = allreduce_max(ms64, world)
-        fp64 = {"value": world * args.fp64_steps / (ms64 / 1000.0), "unit": UNIT,
-                "steps": args.fp64_steps, "warmup": args.fp64_warmup}
-        H64.profile(True)
-        H64.hpsi(p64, hp, occ, stream=stream)
-        fp64["phases_ms_per_H"] = {k: round(v[0], 3) for k, v in H64.profile_read().items() if v[1]}
-        H64.profile(False)
-        del H64, p64
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         cpu = cpu_baseline(args.config, args.cpu_states)
 
     if rank == 0:
+        form_desc = {
+            "mixed_fft64": "FP64 transforms, tensor-core projector GEMMs (FP16 2-piece split, "
+                           "FP32 accumulate per 256, compensated), FP64 kinetic/Taylor/reductions",
+            "mixed": "FP32 transforms, tensor-core projector GEMMs (FP16 2-piece split), FP64 "
+                     "kinetic/Taylor/reductions",
+            "fp64": "FP64 throughout"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "mixed: f32 transforms + f32 projector GEMMs, f64 Taylor sum/reductions",
+                "dtype": "f64 + f16-split tensor GEMM" if args.form != "fp64" else "f64",
+                "form": args.form, "form_desc": form_desc.get(args.form, args.form),
+                "dipole_rel_err_200_steps": acc.get(args.form),
                 "data": "synthetic (seeded cell, random orthonormal states)",
                 "config": {"workload": f"{args.config}: 216 atoms, L=30 bohr, ecut 50 Ry, grid "
                                        f"{cell.grid[0]}^3, {basis.ngw} PW (full sphere), "
@@ -393,9 +438,9 @@ def run_ours(args, rank, world, local):
                            "l2": "inputs (psi 1.1 GB) larger than L2; no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
                 "gpu_launches": launches, "clocks": clk, "roofline": roofline,
-                "e2e": e2e, "fp64_gpu": fp64, "cpu_baseline": cpu}
-        if fp64:
-            line["mixed_over_fp64"] = value / fp64["value"]
+                "e2e": e2e, "other_forms": others, "cpu_baseline": cpu}
+        if "fp64" in others:
+            line["speedup_vs_fp64_gpu"] = value / others["fp64"]["value"]
         print(json.dumps(line), flush=True)
 
 
