@@ -53,7 +53,9 @@ enum {
                                (2-piece FP16 split), FP64 kinetic term, FP64
                                wavefunctions, Taylor sums and reductions */
   QBG_PREC_MIXED_FFT64 = 2, /* as MIXED but FP64 transforms */
-  QBG_PREC_MIXED_NL64 = 3   /* as MIXED but FP64 projector GEMMs */
+  QBG_PREC_MIXED_NL64 = 3,  /* as MIXED but FP64 projector GEMMs */
+  QBG_PREC_MIXED_DF32 = 4   /* as MIXED but double-float (FP32 pair)
+                               transforms: ~48-bit, on the FP32 pipe */
 };
 
 typedef struct qbg_plan qbg_plan;

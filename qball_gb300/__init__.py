@@ -32,8 +32,10 @@ QBG_PREC_FP64 = 0
 QBG_PREC_MIXED = 1
 QBG_PREC_MIXED_FFT64 = 2
 QBG_PREC_MIXED_NL64 = 3
+QBG_PREC_MIXED_DF32 = 4
 PRECISIONS = {"fp64": QBG_PREC_FP64, "mixed": QBG_PREC_MIXED,
-              "mixed_fft64": QBG_PREC_MIXED_FFT64, "mixed_nl64": QBG_PREC_MIXED_NL64}
+              "mixed_fft64": QBG_PREC_MIXED_FFT64, "mixed_nl64": QBG_PREC_MIXED_NL64,
+              "mixed_df32": QBG_PREC_MIXED_DF32}
 _STATUS = {0: "ok", 1: "invalid argument", 2: "out of memory", 3: "unsupported",
            4: "CUDA error", 5: "timeout", 6: "diverged", 7: "bad state"}
 

@@ -385,7 +385,10 @@ static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, doubl
   PhaseTimer pt(p, MODE == Y_VLOC ? PH_Y_VLOC : MODE == Y_DENSITY ? PH_Y_DENSITY
                    : MODE == Y_BWD_STORE ? PH_Y_STORE : PH_Y_LOAD, st);
   const T* v = nullptr;
-  if (MODE == Y_VLOC) v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vr32;
+  if (MODE == Y_VLOC)
+    v = std::is_same<T, double>::value  ? (const T*)p->d_vr
+        : std::is_same<T, float>::value ? (const T*)p->d_vr32
+                                        : (const T*)p->d_vrdf;
   k_y<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((cplx<T>*)p->d_Y, p->nband, p->np0, p->np2,
                                                 p->d_band_y, v, f, w, ns, rho, rho_acc, d);
   QBG_LAUNCHED(p);
@@ -552,5 +555,9 @@ template qbg_status density<double>(qbg_plan*, const double2*, int, int, const d
                                     cudaStream_t);
 template qbg_status density<float>(qbg_plan*, const double2*, int, int, const double*, double*,
                                    cudaStream_t);
+template qbg_status local_hpsi<df32>(qbg_plan*, const double2*, int, double2*, int, bool,
+                                     double2*, int, double2, cudaStream_t);
+template qbg_status density<df32>(qbg_plan*, const double2*, int, int, const double*, double*,
+                                  cudaStream_t);
 
 }  // namespace qbg

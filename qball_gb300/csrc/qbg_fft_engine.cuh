@@ -14,11 +14,14 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "qbg_df32.cuh"
+
 namespace qbg {
 
 template <typename T> struct cplx_of;
 template <> struct cplx_of<double> { using type = double2; };
 template <> struct cplx_of<float> { using type = float2; };
+template <> struct cplx_of<df32> { using type = df32c; };
 template <typename T> using cplx = typename cplx_of<T>::type;
 
 template <typename C> __device__ __forceinline__ C cmk(decltype(C::x) x, decltype(C::x) y) {

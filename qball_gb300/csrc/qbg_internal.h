@@ -38,6 +38,8 @@ struct LenTables {
   double2* d_g64 = nullptr;
   float2* d_tw32 = nullptr;
   float2* d_g32 = nullptr;
+  df32c* d_twdf = nullptr;
+  df32c* d_gdf = nullptr;
   template <typename T> FFTLen<T> view() const;
 };
 
@@ -82,6 +84,7 @@ struct qbg_plan {
   float* d_kpg2A32 = nullptr;        // [ngw]
   double* d_vr = nullptr;            // [N]
   float* d_vr32 = nullptr;           // [N]
+  qbg::df32* d_vrdf = nullptr;       // [N]
   bool have_vr = false;
   std::vector<int> rod_h, rod_k, rod_lmin, rod_size;
   std::vector<double> kpgx_host;

@@ -134,11 +134,14 @@ static qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* ou
   }
   if (p->prec == QBG_PREC_MIXED_FFT64)
     return local_hpsi<double>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
+  if (p->prec == QBG_PREC_MIXED_DF32)
+    return local_hpsi<df32>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
   return local_hpsi<float>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
 }
 
 static bool uses_tc(const qbg_plan* p) {
-  return p->prec == QBG_PREC_MIXED || p->prec == QBG_PREC_MIXED_FFT64;
+  return p->prec == QBG_PREC_MIXED || p->prec == QBG_PREC_MIXED_FFT64 ||
+         p->prec == QBG_PREC_MIXED_DF32;
 }
 
 static qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, const char* who) {
@@ -187,8 +190,13 @@ qbg_status qbg_set_vlocal(qbg_plan* p, const double* v_r) {
   std::vector<double> h(p->N);
   QBG_CUDA(cudaMemcpy(h.data(), p->d_vr, sizeof(double) * p->N, cudaMemcpyDeviceToHost));
   std::vector<float> hf(p->N);
-  for (long long i = 0; i < p->N; ++i) hf[i] = (float)h[i];
+  std::vector<df32> hd(p->N);
+  for (long long i = 0; i < p->N; ++i) {
+    hf[i] = (float)h[i];
+    hd[i] = df32(hf[i], (float)(h[i] - (double)hf[i]));
+  }
   QBG_CUDA(cudaMemcpy(p->d_vr32, hf.data(), sizeof(float) * p->N, cudaMemcpyHostToDevice));
+  QBG_CUDA(cudaMemcpy(p->d_vrdf, hd.data(), sizeof(df32) * p->N, cudaMemcpyHostToDevice));
   p->have_vr = true;
   return QBG_OK;
 }
@@ -293,6 +301,7 @@ static qbg_status density_any(qbg_plan* p, const double2* psi, int ld, int nst,
                               const double* d_w, double* rho, cudaStream_t st) {
   if (p->prec == QBG_PREC_FP64 || p->prec == QBG_PREC_MIXED_FFT64)
     return density<double>(p, psi, ld, nst, d_w, rho, st);
+  if (p->prec == QBG_PREC_MIXED_DF32) return density<df32>(p, psi, ld, nst, d_w, rho, st);
   return density<float>(p, psi, ld, nst, d_w, rho, st);
 }
 

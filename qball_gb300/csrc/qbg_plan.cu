@@ -240,6 +240,35 @@ qbg_status build_len(int n, LenTables& L) {
   std::vector<float2> tw32(ntw), g32(g.size());
   for (int i = 0; i < ntw; ++i) tw32[i] = make_float2((float)tw[i].x, (float)tw[i].y);
   for (size_t i = 0; i < g.size(); ++i) g32[i] = make_float2((float)g[i].x, (float)g[i].y);
+  // double-float tables from the extended-precision values
+  auto to_df = [](long double v) {
+    const float h = (float)v;
+    return df32(h, (float)(v - (long double)h));
+  };
+  std::vector<df32c> twdf(ntw), gdf(g.size());
+  for (int p = 0; p < L.npass; ++p) {
+    const int R = L.radix[p], Ns = L.ns[p];
+    for (int k = 0; k < Ns; ++k)
+      for (int r = 0; r < R; ++r) {
+        const long long t = ((long long)r * k) % ((long long)Ns * R);
+        const long double pi = 3.14159265358979323846264338327950288L;
+        const long double ang = 2.0L * pi * (long double)t / (long double)(Ns * R);
+        twdf[L.twoff[p] + k * R + r] = df32c{to_df(std::cos(ang)), to_df(-std::sin(ang))};
+      }
+  }
+  {
+    const int ps[3] = {7, 11, 13}, off[3] = {0, 7, 18};
+    for (int q = 0; q < 3; ++q)
+      for (int m = 0; m < ps[q]; ++m) {
+        const long double pi = 3.14159265358979323846264338327950288L;
+        const long double ang = 2.0L * pi * (long double)m / (long double)ps[q];
+        gdf[off[q] + m] = df32c{to_df(std::cos(ang)), to_df(-std::sin(ang))};
+      }
+  }
+  QBG_CUDA(cudaMalloc(&L.d_twdf, sizeof(df32c) * ntw));
+  QBG_CUDA(cudaMalloc(&L.d_gdf, sizeof(df32c) * gdf.size()));
+  QBG_CUDA(cudaMemcpy(L.d_twdf, twdf.data(), sizeof(df32c) * ntw, cudaMemcpyHostToDevice));
+  QBG_CUDA(cudaMemcpy(L.d_gdf, gdf.data(), sizeof(df32c) * gdf.size(), cudaMemcpyHostToDevice));
   QBG_CUDA(cudaMalloc(&L.d_tw64, sizeof(double2) * ntw));
   QBG_CUDA(cudaMalloc(&L.d_tw32, sizeof(float2) * ntw));
   QBG_CUDA(cudaMalloc(&L.d_g64, sizeof(double2) * g.size()));
@@ -256,6 +285,10 @@ void free_len(LenTables& L) {
   cudaFree(L.d_tw32);
   cudaFree(L.d_g64);
   cudaFree(L.d_g32);
+  cudaFree(L.d_twdf);
+  cudaFree(L.d_gdf);
+  L.d_twdf = nullptr;
+  L.d_gdf = nullptr;
   L.d_tw64 = nullptr;
   L.d_tw32 = nullptr;
   L.d_g64 = nullptr;
@@ -280,6 +313,22 @@ template <> FFTLen<double> LenTables::view<double>() const {
   }
   d.tw = d_tw64;
   d.gtab = d_g64;
+  d.goff7 = goff7;
+  d.goff11 = goff11;
+  d.goff13 = goff13;
+  return d;
+}
+template <> FFTLen<df32> LenTables::view<df32>() const {
+  FFTLen<df32> d;
+  d.n = n;
+  d.npass = npass;
+  for (int i = 0; i < kMaxPass; ++i) {
+    d.radix[i] = radix[i];
+    d.ns[i] = ns[i];
+    d.twoff[i] = twoff[i];
+  }
+  d.tw = d_twdf;
+  d.gtab = d_gdf;
   d.goff7 = goff7;
   d.goff11 = goff11;
   d.goff13 = goff13;
@@ -365,7 +414,7 @@ qbg_status qbg_plan_destroy(qbg_plan* p) {
   tc_release(p);
   for (auto& L : p->len) free_len(L);
   void* bufs[] = {p->d_rods, p->d_row_ptr, p->d_row_rod, p->d_row_x, p->d_band_y,
-                  p->d_kpgx, p->d_kpg2A, p->d_kpg2A32, p->d_vr, p->d_vr32,
+                  p->d_kpgx, p->d_kpg2A, p->d_kpg2A32, p->d_vr, p->d_vr32, p->d_vrdf,
                   p->d_plist, p->d_ptau, p->d_pwt, p->d_pl, p->d_prc,
                   p->d_anl, p->d_anl32, p->d_Z, p->d_Y, p->d_fnl, p->d_fpart,
                   p->d_red, p->d_rho, p->d_w[0], p->d_w[1], p->d_w[2], p->d_w[3]};
@@ -380,7 +429,7 @@ qbg_status qbg_plan_create(const qbg_basis_desc* bd, int np0, int np1, int np2,
                            int precision, qbg_plan** out) {
   if (!bd || !out || bd->ngw < 0 || bd->nrods < 0 || np0 <= 0 || np1 <= 0 || np2 <= 0 ||
       (bd->ngw > 0 && (!bd->rod_h || !bd->rod_k || !bd->rod_lmin || !bd->rod_size || !bd->kpgx)) ||
-      precision < QBG_PREC_FP64 || precision > QBG_PREC_MIXED_NL64 || !(bd->omega > 0.0)) {
+      precision < QBG_PREC_FP64 || precision > QBG_PREC_MIXED_DF32 || !(bd->omega > 0.0)) {
     set_error("qbg_plan_create: invalid argument");
     return QBG_ERR_INVALID;
   }
@@ -484,6 +533,8 @@ qbg_status qbg_plan_create(const qbg_basis_desc* bd, int np0, int np1, int np2,
   }
   cudaError_t e = cudaMalloc(&p->d_vr, sizeof(double) * p->N);
   if (e == cudaSuccess) e = cudaMalloc(&p->d_vr32, sizeof(float) * p->N);
+  if (e == cudaSuccess) e = cudaMalloc(&p->d_vrdf, sizeof(df32) * p->N);
+  if (e == cudaSuccess) e = cudaMemset(p->d_vrdf, 0, sizeof(df32) * p->N);
   if (e == cudaSuccess) e = cudaMemset(p->d_vr, 0, sizeof(double) * p->N);
   if (e == cudaSuccess) e = cudaMemset(p->d_vr32, 0, sizeof(float) * p->N);
   if (e != cudaSuccess) {
@@ -491,7 +542,7 @@ qbg_status qbg_plan_create(const qbg_basis_desc* bd, int np0, int np1, int np2,
     qbg_plan_destroy(p);
     return st;
   }
-  p->chunk = (precision == QBG_PREC_FP64 || precision == QBG_PREC_MIXED_FFT64) ? 8 : 16;
+  p->chunk = (precision == QBG_PREC_MIXED || precision == QBG_PREC_MIXED_NL64) ? 16 : 8;
   *out = p;
   return QBG_OK;
 }

@@ -200,11 +200,13 @@ def test_etrs_time_dependent_vector_potential(cuda):
     assert rel_err(p.cpu().numpy(), ref.T) < 1e-10
 
 
-@pytest.mark.parametrize("name", ["t12", "c1"])
-def test_hpsi_mixed_vs_oracle(cuda, name):
-    """FP32 transforms + tensor-core projector GEMMs (2-piece FP16 split),
-    FP64 kinetic term and FP64 in/out: <= 2e-6 relative to the FP64 oracle."""
-    cell, b, H, oft, oh, psi = setup(name, prec="mixed")
+@pytest.mark.parametrize("name,prec", [("t12", "mixed"), ("c1", "mixed"), ("c1", "mixed_fft64"),
+                                       ("c1", "mixed_df32"), ("t12b", "mixed_nl64")])
+def test_hpsi_mixed_vs_oracle(cuda, name, prec):
+    """Reduced-precision forms (tensor-core projector GEMMs with a 2-piece FP16
+    split and/or FP32 or double-float transforms; FP64 kinetic term and FP64
+    in/out): <= 2e-6 relative to the FP64 oracle."""
+    cell, b, H, oft, oh, psi = setup(name, prec=prec)
     occ = synth.occupations(cell)
     torch = _torch()
     out = torch.zeros_like(dev(psi))
@@ -215,7 +217,7 @@ def test_hpsi_mixed_vs_oracle(cuda, name):
     assert abs(enl - enl_ref) <= 2e-6 * abs(enl_ref)
     # the nonlocal part alone through the tensor cores
     parts, _ = oh.parts(psi.T, occ, nthreads=NT)
-    Hloc = Q.Hamiltonian(b, *cell.grid, precision="mixed")
+    Hloc = Q.Hamiltonian(b, *cell.grid, precision=prec)
     Hloc.set_vlocal(np.zeros(oft.n012))
     Hloc.set_nonlocal(synth.species(cell))
     out2 = torch.zeros_like(out)
@@ -244,3 +246,21 @@ def test_unsupported_and_too_small_grids(cuda):
         Q.FourierTransform(b, 34, 32, 32)   # 34 = 2*17
     with pytest.raises(Q.QbgError, match="invalid"):
         Q.FourierTransform(b, 16, 16, 16)   # sphere does not fit
+
+
+def test_df32_transforms_match_fp64_closely(cuda):
+    """The double-float transforms carry ~48 bits: the local part of H psi
+    agrees with the FP64 form to ~1e-12."""
+    cell = synth.make_cell("c1")
+    b = Q.Basis(cell.L, cell.ecut)
+    v = synth.vlocal(cell)
+    psi = synth.wavefunctions(cell, b)
+    outs = {}
+    torch = _torch()
+    for prec in ("fp64", "mixed_df32"):
+        H = Q.Hamiltonian(b, *cell.grid, precision=prec)
+        H.set_vlocal(v)
+        o = torch.zeros_like(dev(psi))
+        H.hpsi(dev(psi), o, synth.occupations(cell))
+        outs[prec] = o.cpu().numpy()
+    assert rel_err(outs["mixed_df32"], outs["fp64"]) < 1e-11
