@@ -1,12 +1,12 @@
 #!/usr/bin/env python3
 """ETRS steps/s on the 216-atom cell: mixed precision vs the plain FP64 form.
 
-`value` times the precision form given by --form (default mixed_fft64: FP64
-transforms, projector GEMMs on the tensor cores) -- the fastest form whose
-200-step dipole stays within 1e-8 (relative) of the plain FP64 form
-(profiles/accuracy.json, produced by python -m qball_gb300.accuracy).  The
-FP32-transform form (--also, default mixed) and the plain FP64 form are timed
-beside it under `other_forms`.
+`value` times the precision form given by --form (default mixed_df32:
+double-float transforms on the FP32 pipe, projector GEMMs on the tensor
+cores) -- the fastest form whose 200-step dipole stays within 1e-8 (relative)
+of the plain FP64 form (profiles/accuracy.json, produced by python -m
+qball_gb300.accuracy).  The FP32-transform form, the FP64-transform form and
+the plain FP64 form are timed beside it under `other_forms`.
 
 One "step" is one ETRS step of ExponentialWavefunctionStepper (preupdate +
 update: three 4th-order Taylor exponentials = 12 H|psi> applications, plus
@@ -57,10 +57,11 @@ def parse():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--chunk", type=int, default=0)
-    ap.add_argument("--form", default="mixed_fft64",
+    ap.add_argument("--form", default="mixed_df32",
                     help="precision form timed for `value` (the fastest form whose 200-step "
                          "dipole error is within 1e-8 of the FP64 form)")
-    ap.add_argument("--also", default="mixed", help="a second form timed beside it")
+    ap.add_argument("--also", default="mixed,mixed_fft64",
+                    help="comma-separated forms timed beside it")
     ap.add_argument("--also-steps", type=int, default=3)
     ap.add_argument("--also-warmup", type=int, default=3)
     return ap.parse_args()
@@ -394,8 +395,9 @@ def run_ours(args, rank, world, local):
 
     # the other forms on the same cell and states
     others = {}
-    for form, steps, warm in ((args.also, args.also_steps, args.also_warmup),
-                              ("fp64", args.fp64_steps, args.fp64_warmup)):
+    runs = [(f, args.also_steps, args.also_warmup) for f in args.also.split(",") if f]
+    runs.append(("fp64", args.fp64_steps, args.fp64_warmup))
+    for form, steps, warm in runs:
         if not form or (form == "fp64" and args.skip_fp64):
             continue
         _, _, H2, _ = make_system(args.config, form, psi_np=psi)
@@ -419,6 +421,9 @@ def run_ours(args, rank, world, local):
 
     if rank == 0:
         form_desc = {
+            "mixed_df32": "double-float (FP32 pair) transforms, tensor-core projector GEMMs "
+                          "(FP16 2-piece split, compensated accumulation), FP64 kinetic/Taylor/"
+                          "reductions",
             "mixed_fft64": "FP64 transforms, tensor-core projector GEMMs (FP16 2-piece split, "
                            "FP32 accumulate per 256, compensated), FP64 kinetic/Taylor/reductions",
             "mixed": "FP32 transforms, tensor-core projector GEMMs (FP16 2-piece split), FP64 "
