@@ -46,6 +46,7 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
   const int n2 = d.n, ls = n2 + 1;
   C* A = reinterpret_cast<C*>(smem);
   C* B = A + kTile * ls;
+  const FFTLen<T> dv = stage_twiddles<T>(d, B + kTile * ls, BIGP);
   const int r0 = blockIdx.x * kTile;
   const int nl = min(kTile, nrods - r0);
   const double2* ps = psi + (size_t)blockIdx.y * ld;
@@ -65,7 +66,7 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
     }
   }
   __syncthreads();
-  const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, d);
+  const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
   C* Zs = Z + (size_t)blockIdx.y * n2 * nrods;
   for (int it = threadIdx.x; it < nl * n2; it += blockDim.x) {
     const int rl = it % nl, z = it / nl;
@@ -91,6 +92,7 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
   const int n2 = d.n, ls = n2 + 1;
   C* A = reinterpret_cast<C*>(smem);
   C* B = A + kTile * ls;
+  const FFTLen<T> dv = stage_twiddles<T>(d, B + kTile * ls, BIGP);
   const int r0 = blockIdx.x * kTile;
   const int nl = min(kTile, nrods - r0);
   const int s = blockIdx.y;
@@ -100,7 +102,7 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
     A[rl * ls + z] = Zs[(size_t)z * nrods + r0 + rl];
   }
   __syncthreads();
-  const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
+  const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double2* os = out + (size_t)s * ldo;
   for (int rl = warp; rl < nl; rl += nw) {
@@ -149,6 +151,7 @@ k_x_bwd(const cplx<T>* __restrict__ Z, cplx<T>* __restrict__ Y, int nrods,
   const int n0 = d.n, ls = n0 + 1;
   C* A = reinterpret_cast<C*>(smem);
   C* B = A + kTile * ls;
+  const FFTLen<T> dv = stage_twiddles<T>(d, B + kTile * ls, BIGP);
   const int nbt = (nband + kTile - 1) / kTile;
   const int z = blockIdx.x / nbt;
   const int b0 = (blockIdx.x % nbt) * kTile;
@@ -163,7 +166,7 @@ k_x_bwd(const cplx<T>* __restrict__ Z, cplx<T>* __restrict__ Y, int nrods,
     A[((xb >> 16) - b0) * ls + (xb & 0xffff)] = Zr[row_rod[q]];
   }
   __syncthreads();
-  const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, d);
+  const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
   C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
   for (int it = threadIdx.x; it < nl * n0; it += blockDim.x) {
     const int bl = it / n0, x = it - bl * n0;
@@ -182,6 +185,7 @@ k_x_fwd(const cplx<T>* __restrict__ Y, cplx<T>* __restrict__ Z, int nrods,
   const int n0 = d.n, ls = n0 + 1;
   C* A = reinterpret_cast<C*>(smem);
   C* B = A + kTile * ls;
+  const FFTLen<T> dv = stage_twiddles<T>(d, B + kTile * ls, BIGP);
   const int nbt = (nband + kTile - 1) / kTile;
   const int z = blockIdx.x / nbt;
   const int b0 = (blockIdx.x % nbt) * kTile;
@@ -193,7 +197,7 @@ k_x_fwd(const cplx<T>* __restrict__ Y, cplx<T>* __restrict__ Z, int nrods,
     A[bl * ls + x] = Yp[(size_t)(b0 + bl) * n0 + x];
   }
   __syncthreads();
-  const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
+  const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
   C* Zr = Z + ((size_t)s * n2 + z) * nrods;
   const int q1 = row_ptr[b0 + nl];
   for (int q = row_ptr[b0] + threadIdx.x; q < q1; q += blockDim.x) {
@@ -217,6 +221,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
   const int n1 = d.n, ls = n1 + 1;
   C* A = reinterpret_cast<C*>(smem);
   C* B = A + kTile * ls;
+  const FFTLen<T> dv = stage_twiddles<T>(d, B + kTile * ls, BIGP);
   const int nct = (n0 + kTile - 1) / kTile;
   const int z = blockIdx.x / nct;
   const int x0 = (blockIdx.x % nct) * kTile;
@@ -241,7 +246,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
         A[cl * ls + y] = c;
       }
       __syncthreads();
-      R = fft_lines<-1, T, BIGP>(A, B, nl, ls, d);
+      R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
     } else {
       for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
       __syncthreads();
@@ -250,7 +255,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
         A[cl * ls + band_y[b]] = Yp[(size_t)b * n0 + x0 + cl];
       }
       __syncthreads();
-      R = fft_lines<+1, T, BIGP>(A, B, nl, ls, d);
+      R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
     }
     if (MODE == Y_VLOC) {
       const T* vz = v + (size_t)z * plane;
@@ -264,7 +269,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
       }
       __syncthreads();
       C* other = R == A ? B : A;
-      R = fft_lines<-1, T, BIGP>(R, other, nl, ls, d);
+      R = fft_lines<-1, T, BIGP>(R, other, nl, ls, dv);
     }
     if (MODE == Y_BWD_STORE) {
       double2* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
@@ -309,8 +314,8 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
 }
 
 // ------------------------------------------------------------- launchers
-template <typename T> static size_t smem_bytes(int n) {
-  return 2 * (size_t)kTile * (n + 1) * sizeof(cplx<T>);
+template <typename T> static size_t smem_bytes(const FFTLen<T>& d) {
+  return (2 * (size_t)kTile * (d.n + 1) + d.ntw + kGtab) * sizeof(cplx<T>);
 }
 
 template <typename K> static cudaError_t prep(K kernel, size_t smem) {
@@ -336,7 +341,7 @@ static bool big_prime(const LenTables& L) {
 template <typename T, bool BIGP>
 static qbg_status run_z_bwd_(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st) {
   const FFTLen<T> d = p->len[2].view<T>();
-  const size_t sm = smem_bytes<T>(d.n);
+  const size_t sm = smem_bytes<T>(d);
   QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   PhaseTimer pt(p, PH_Z_BWD, st);
@@ -353,7 +358,7 @@ static qbg_status run_z_bwd(qbg_plan* p, const double2* c, int ldc, int ns, cuda
 template <typename T, bool BIGP>
 static qbg_status run_x_(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
   const FFTLen<T> d = p->len[0].view<T>();
-  const size_t sm = smem_bytes<T>(d.n);
+  const size_t sm = smem_bytes<T>(d);
   dim3 grid(p->np2 * ((p->nband + kTile - 1) / kTile), ns);
   PhaseTimer pt(p, bwd ? PH_X_BWD : PH_X_FWD, st);
   if (bwd) {
@@ -379,7 +384,7 @@ template <typename T, int MODE, bool BIGP>
 static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, double* rho,
                          int rho_acc, cudaStream_t st) {
   const FFTLen<T> d = p->len[1].view<T>();
-  const size_t sm = smem_bytes<T>(d.n);
+  const size_t sm = smem_bytes<T>(d);
   QBG_CUDA(prep(k_y<T, MODE, BIGP>, sm));
   dim3 grid(p->np2 * ((p->np0 + kTile - 1) / kTile), MODE == Y_DENSITY ? 1 : ns);
   PhaseTimer pt(p, MODE == Y_VLOC ? PH_Y_VLOC : MODE == Y_DENSITY ? PH_Y_DENSITY
@@ -406,7 +411,7 @@ static qbg_status run_z_fwd_(qbg_plan* p, double2* out, int ldo, int ns, const d
                              int ldp, int out_init, double2* acc, int lda, double2 fac,
                              cudaStream_t st) {
   const FFTLen<T> d = p->len[2].view<T>();
-  const size_t sm = smem_bytes<T>(d.n);
+  const size_t sm = smem_bytes<T>(d);
   QBG_CUDA(prep(k_z_fwd<T, MODE, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   const T scale = (T)(1.0 / (double)(p->np0 * p->np1 * p->np2));
@@ -503,7 +508,7 @@ template <typename T, bool BX, bool BY, bool BZ>
 static qbg_status backward_scratch_(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,
                                     cplx<T>* Z, cplx<T>* Y, int chunk, cudaStream_t st) {
   const FFTLen<T> dz = p->len[2].view<T>(), dx = p->len[0].view<T>(), dy = p->len[1].view<T>();
-  const size_t smz = smem_bytes<T>(dz.n), smx = smem_bytes<T>(dx.n), smy = smem_bytes<T>(dy.n);
+  const size_t smz = smem_bytes<T>(dz), smx = smem_bytes<T>(dx), smy = smem_bytes<T>(dy);
   QBG_CUDA(prep(k_z_bwd<T, BZ>, smz));
   QBG_CUDA(prep(k_x_bwd<T, BX>, smx));
   QBG_CUDA((prep(k_y<T, Y_BWD_STORE, BY>, smy)));

@@ -24,19 +24,19 @@ template <> struct cplx_of<float> { using type = float2; };
 template <> struct cplx_of<df32> { using type = df32c; };
 template <typename T> using cplx = typename cplx_of<T>::type;
 
-template <typename C> __device__ __forceinline__ C cmk(decltype(C::x) x, decltype(C::x) y) {
+template <typename C> __host__ __device__ __forceinline__ C cmk(decltype(C::x) x, decltype(C::x) y) {
   C c; c.x = x; c.y = y; return c;
 }
-template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return cmk<C>(a.x + b.x, a.y + b.y); }
-template <typename C> __device__ __forceinline__ C csub(C a, C b) { return cmk<C>(a.x - b.x, a.y - b.y); }
-template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+template <typename C> __host__ __device__ __forceinline__ C cadd(C a, C b) { return cmk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __host__ __device__ __forceinline__ C csub(C a, C b) { return cmk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __host__ __device__ __forceinline__ C cmul(C a, C b) {
   return cmk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
-template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {  // a * conj(b)
+template <typename C> __host__ __device__ __forceinline__ C cmulc(C a, C b) {  // a * conj(b)
   return cmk<C>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
 }
 // multiply by S*i : S=+1 -> i*(x+iy) = (-y, x); S=-1 -> (y, -x)
-template <int S, typename C> __device__ __forceinline__ C cmul_si(C a) {
+template <int S, typename C> __host__ __device__ __forceinline__ C cmul_si(C a) {
   return S > 0 ? cmk<C>(-a.y, a.x) : cmk<C>(a.y, -a.x);
 }
 
@@ -49,19 +49,44 @@ template <typename T> struct FFTLen {
   int radix[kMaxPass];
   int ns[kMaxPass];     // product of the radices of the passes before
   int twoff[kMaxPass];  // offset of the pass' twiddles in tw
+  float inv_m[kMaxPass];   // 1 / (n / radix)
+  float inv_ns[kMaxPass];  // 1 / ns
+  int ntw;                 // twiddle table length
   const cplx<T>* tw;    // exp(-2 pi i r k / (ns*radix)), k<ns, r<radix
   const cplx<T>* gtab;  // exp(-2 pi i m / p) for the direct-DFT primes
   int goff7, goff11, goff13;
 };
 
+constexpr int kGtab = 31;  // 7 + 11 + 13 direct-DFT roots
+
+// floor(a / b) for 0 <= a < 2^20 and 1 <= b <= 2^12 with inv = 1/b rounded
+// to FP32: the product's error is far below the gap to the next integer
+__device__ __forceinline__ int fdiv(int a, float inv) {
+  return (int)(((float)a + 0.5f) * inv);
+}
+
+// Copies the length's twiddle tables into shared memory (dst holds
+// ntw + kGtab entries) and returns a view that reads them from there.  The
+// caller synchronises before the first pass.
+template <typename T>
+__device__ __forceinline__ FFTLen<T> stage_twiddles(const FFTLen<T>& d, cplx<T>* dst, bool bigp) {
+  for (int i = threadIdx.x; i < d.ntw; i += blockDim.x) dst[i] = d.tw[i];
+  if (bigp)
+    for (int i = threadIdx.x; i < kGtab; i += blockDim.x) dst[d.ntw + i] = d.gtab[i];
+  FFTLen<T> v = d;
+  v.tw = dst;
+  if (bigp) v.gtab = dst + d.ntw;
+  return v;
+}
+
 // ---------------------------------------------------------------- codelets
-template <int S, typename C> __device__ __forceinline__ void dft2(C* v) {
+template <int S, typename C> __host__ __device__ __forceinline__ void dft2(C* v) {
   C a = v[0], b = v[1];
   v[0] = cadd(a, b);
   v[1] = csub(a, b);
 }
 
-template <int S, typename C> __device__ __forceinline__ void dft3(C* v) {
+template <int S, typename C> __host__ __device__ __forceinline__ void dft3(C* v) {
   using T = decltype(C::x);
   const T h = T(0.86602540378443864676372317075293618);  // sin(2 pi/3)
   C t1 = cadd(v[1], v[2]);
@@ -73,7 +98,7 @@ template <int S, typename C> __device__ __forceinline__ void dft3(C* v) {
   v[2] = csub(t2, t3);
 }
 
-template <int S, typename C> __device__ __forceinline__ void dft4(C* v) {
+template <int S, typename C> __host__ __device__ __forceinline__ void dft4(C* v) {
   C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
   C c = cadd(v[1], v[3]), d = cmul_si<S>(csub(v[1], v[3]));
   v[0] = cadd(a, c);
@@ -82,7 +107,7 @@ template <int S, typename C> __device__ __forceinline__ void dft4(C* v) {
   v[3] = csub(b, d);
 }
 
-template <int S, typename C> __device__ __forceinline__ void dft5(C* v) {
+template <int S, typename C> __host__ __device__ __forceinline__ void dft5(C* v) {
   using T = decltype(C::x);
   const T c1 = T(0.30901699437494742410229341718281906);   // cos(2 pi/5)
   const T c2 = T(-0.80901699437494742410229341718281906);  // cos(4 pi/5)
@@ -102,7 +127,7 @@ template <int S, typename C> __device__ __forceinline__ void dft5(C* v) {
   v[3] = csub(t2, u2);
 }
 
-template <int S, typename C> __device__ __forceinline__ void dft8(C* v) {
+template <int S, typename C> __host__ __device__ __forceinline__ void dft8(C* v) {
   using T = decltype(C::x);
   const T r2 = T(0.70710678118654752440084436210484904);
   C e[4] = {v[0], v[2], v[4], v[6]};
@@ -124,7 +149,7 @@ template <int S, typename C> __device__ __forceinline__ void dft8(C* v) {
 
 // direct DFT for a small prime p with table g[m] = exp(-2 pi i m/p)
 template <int P, int S, typename C>
-__device__ __forceinline__ void dftp(C* v, const C* g) {
+__host__ __device__ __forceinline__ void dftp(C* v, const C* g) {
   C y[P];
 #pragma unroll
   for (int k = 0; k < P; ++k) {
@@ -141,6 +166,111 @@ __device__ __forceinline__ void dftp(C* v, const C* g) {
   for (int k = 0; k < P; ++k) v[k] = y[k];
 }
 
+// multiply by the constant exp(S*2*pi*i*e/n) given as (c, s) = (cos, sin)
+template <int S, typename C>
+__host__ __device__ __forceinline__ C cmul_root(C a, double c, double sn) {
+  using T = decltype(C::x);
+  const T cr = T(c), ci = T(S * sn);
+  return cmk<C>(a.x * cr - a.y * ci, a.x * ci + a.y * cr);
+}
+
+// 16 = 4 x 4: X[c+4d] = sum_b W4^{bd} W16^{bc} sum_a x[4a+b] W4^{ac}
+template <int S, typename C> __host__ __device__ __forceinline__ void dft16(C* v) {
+  const double c1 = 0.92387953251128675612818318939678829, s1 = 0.38268343236508977172845998403039887;
+  const double r2 = 0.70710678118654752440084436210484904;
+  C y[4][4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    C t[4] = {v[b], v[4 + b], v[8 + b], v[12 + b]};
+    dft4<S>(t);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) y[b][c] = t[c];
+  }
+  // twiddles W16^{bc}
+  y[1][1] = cmul_root<S>(y[1][1], c1, s1);
+  y[1][2] = cmul_root<S>(y[1][2], r2, r2);
+  y[1][3] = cmul_root<S>(y[1][3], s1, c1);
+  y[2][1] = cmul_root<S>(y[2][1], r2, r2);
+  y[2][2] = cmul_si<S>(y[2][2]);
+  y[2][3] = cmul_root<S>(y[2][3], -r2, r2);
+  y[3][1] = cmul_root<S>(y[3][1], s1, c1);
+  y[3][2] = cmul_root<S>(y[3][2], -r2, r2);
+  y[3][3] = cmul_root<S>(y[3][3], -c1, -s1);
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    C t[4] = {y[0][c], y[1][c], y[2][c], y[3][c]};
+    dft4<S>(t);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) v[c + 4 * d] = t[d];
+  }
+}
+
+// 9 = 3 x 3 with twiddles W9^{bc}
+template <int S, typename C> __host__ __device__ __forceinline__ void dft9(C* v) {
+  const double c1 = 0.76604444311897803520239265055541667, s1 = 0.64278760968653932632264340990726344;  // 2pi/9
+  const double c2 = 0.17364817766693034885171662676931480, s2 = 0.98480775301220805936674302458952301;  // 4pi/9
+  const double c4 = -0.93969262078590838405410927732473147, s4 = 0.34202014332566873304409961468225958; // 8pi/9
+  C y[3][3];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    C t[3] = {v[b], v[3 + b], v[6 + b]};
+    dft3<S>(t);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) y[b][c] = t[c];
+  }
+  y[1][1] = cmul_root<S>(y[1][1], c1, s1);
+  y[1][2] = cmul_root<S>(y[1][2], c2, s2);
+  y[2][1] = cmul_root<S>(y[2][1], c2, s2);
+  y[2][2] = cmul_root<S>(y[2][2], c4, s4);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    C t[3] = {y[0][c], y[1][c], y[2][c]};
+    dft3<S>(t);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v[c + 3 * d] = t[d];
+  }
+}
+
+// Good-Thomas prime-factor DFT of N = N1*N2 (coprime): input n = (N2 n1 + N1 n2)
+// mod N, output k with k = k1 (mod N1), k = k2 (mod N2) -- a 2-D DFT without
+// twiddles.  K1, K2 are the CRT coefficients (k = K1 k1 + K2 k2 mod N).
+template <int S, int N1, int N2, int K1, int K2, typename C, typename F1, typename F2>
+__host__ __device__ __forceinline__ void dft_pfa(C* v, F1 f1, F2 f2) {
+  constexpr int N = N1 * N2;
+  C y[N1][N2];
+#pragma unroll
+  for (int n1 = 0; n1 < N1; ++n1) {
+    C t[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) t[n2] = v[(N2 * n1 + N1 * n2) % N];
+    f2(t);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) y[n1][k2] = t[k2];
+  }
+#pragma unroll
+  for (int k2 = 0; k2 < N2; ++k2) {
+    C t[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) t[n1] = y[n1][k2];
+    f1(t);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) v[(K1 * k1 + K2 * k2) % N] = t[k1];
+  }
+}
+
+template <int S, typename C> __host__ __device__ __forceinline__ void dft15(C* v) {
+  dft_pfa<S, 3, 5, 10, 6>(v, [](C* t) { dft3<S>(t); }, [](C* t) { dft5<S>(t); });
+}
+template <int S, typename C> __host__ __device__ __forceinline__ void dft10(C* v) {
+  dft_pfa<S, 2, 5, 5, 6>(v, [](C* t) { dft2<S>(t); }, [](C* t) { dft5<S>(t); });
+}
+template <int S, typename C> __host__ __device__ __forceinline__ void dft6(C* v) {
+  dft_pfa<S, 2, 3, 3, 4>(v, [](C* t) { dft2<S>(t); }, [](C* t) { dft3<S>(t); });
+}
+template <int S, typename C> __host__ __device__ __forceinline__ void dft12(C* v) {
+  dft_pfa<S, 4, 3, 9, 4>(v, [](C* t) { dft4<S>(t); }, [](C* t) { dft3<S>(t); });
+}
+
 template <int R, int S, typename C>
 __device__ __forceinline__ void dft_r(C* v, const C* gtab, int g7, int g11, int g13) {
   if constexpr (R == 2) dft2<S>(v);
@@ -148,6 +278,12 @@ __device__ __forceinline__ void dft_r(C* v, const C* gtab, int g7, int g11, int 
   else if constexpr (R == 4) dft4<S>(v);
   else if constexpr (R == 5) dft5<S>(v);
   else if constexpr (R == 8) dft8<S>(v);
+  else if constexpr (R == 16) dft16<S>(v);
+  else if constexpr (R == 9) dft9<S>(v);
+  else if constexpr (R == 6) dft6<S>(v);
+  else if constexpr (R == 10) dft10<S>(v);
+  else if constexpr (R == 12) dft12<S>(v);
+  else if constexpr (R == 15) dft15<S>(v);
   else if constexpr (R == 7) dftp<7, S>(v, gtab + g7);
   else if constexpr (R == 11) dftp<11, S>(v, gtab + g11);
   else if constexpr (R == 13) dftp<13, S>(v, gtab + g13);
@@ -164,14 +300,15 @@ __device__ __forceinline__ void fft_pass(const cplx<T>* __restrict__ src,
   const int Ns = d.ns[p];
   const C* tw = d.tw + d.twoff[p];
   const int items = nlines * m;
+  const float inv_m = d.inv_m[p], inv_ns = d.inv_ns[p];
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
-    const int line = it / m;
+    const int line = fdiv(it, inv_m);
     const int j = it - line * m;
     const C* s = src + line * ls;
     C v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = s[j + r * m];
-    const int k = j % Ns;
+    const int k = j - fdiv(j, inv_ns) * Ns;
     if (Ns > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
@@ -200,6 +337,12 @@ __device__ cplx<T>* fft_lines(cplx<T>* A, cplx<T>* B, int nlines, int ls,
       case 4: fft_pass<4, S, T>(A, B, nlines, ls, d, p); break;
       case 5: fft_pass<5, S, T>(A, B, nlines, ls, d, p); break;
       case 8: fft_pass<8, S, T>(A, B, nlines, ls, d, p); break;
+      case 16: fft_pass<16, S, T>(A, B, nlines, ls, d, p); break;
+      case 9: fft_pass<9, S, T>(A, B, nlines, ls, d, p); break;
+      case 6: fft_pass<6, S, T>(A, B, nlines, ls, d, p); break;
+      case 10: fft_pass<10, S, T>(A, B, nlines, ls, d, p); break;
+      case 12: fft_pass<12, S, T>(A, B, nlines, ls, d, p); break;
+      case 15: fft_pass<15, S, T>(A, B, nlines, ls, d, p); break;
       case 7: if constexpr (BIGP) fft_pass<7, S, T>(A, B, nlines, ls, d, p); break;
       case 11: if constexpr (BIGP) fft_pass<11, S, T>(A, B, nlines, ls, d, p); break;
       case 13: if constexpr (BIGP) fft_pass<13, S, T>(A, B, nlines, ls, d, p); break;

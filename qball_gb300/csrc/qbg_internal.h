@@ -34,6 +34,7 @@ struct LenTables {
   int ns[kMaxPass] = {0};
   int twoff[kMaxPass] = {0};
   int goff7 = 0, goff11 = 0, goff13 = 0;
+  int ntw = 0;
   double2* d_tw64 = nullptr;
   double2* d_g64 = nullptr;
   float2* d_tw32 = nullptr;

@@ -183,14 +183,40 @@ std::vector<Rod> build_rods(const double* a, double ecut, int* info) {
 }
 
 // ------------------------------------------------------- transform tables
+// Radices with a hand-written codelet (7, 11, 13 are direct DFTs).
+bool is_codelet(int r) {
+  switch (r) {
+    case 2: case 3: case 4: case 5: case 6: case 7: case 8: case 9:
+    case 10: case 11: case 12: case 13: case 15: case 16: return true;
+    default: return false;
+  }
+}
+
+// Two passes when n = R1 * R2 with both codelets (power-of-two first), else
+// the greedy 8/4/2/odd-prime split.
 bool factorize(int n, LenTables& L) {
-  int r[16], np = 0, m = n;
-  while (m % 8 == 0 && m > 1 && np < 16) { r[np++] = 8; m /= 8; }
-  if (m % 4 == 0) { r[np++] = 4; m /= 4; }
-  if (m % 2 == 0) { r[np++] = 2; m /= 2; }
-  for (int q : {3, 5, 7, 11, 13})
-    while (m % q == 0 && np < 16) { r[np++] = q; m /= q; }
-  if (m != 1 || np > kMaxPass) return false;
+  int r[16], np = 0;
+  if (is_codelet(n)) {
+    r[np++] = n;
+  } else {
+    for (int r1 : {16, 8, 4, 2, 12, 10, 9, 6, 15}) {
+      if (n % r1 == 0 && is_codelet(n / r1)) {
+        r[np++] = r1;
+        r[np++] = n / r1;
+        break;
+      }
+    }
+  }
+  if (np == 0) {
+    int m = n;
+    while (m % 8 == 0 && m > 1 && np < 16) { r[np++] = 8; m /= 8; }
+    if (m % 4 == 0) { r[np++] = 4; m /= 4; }
+    if (m % 2 == 0) { r[np++] = 2; m /= 2; }
+    for (int q : {3, 5, 7, 11, 13})
+      while (m % q == 0 && np < 16) { r[np++] = q; m /= q; }
+    if (m != 1) return false;
+  }
+  if (np > kMaxPass) return false;
   L.n = n;
   L.npass = np;
   int ns = 1, off = 0;
@@ -220,6 +246,7 @@ qbg_status build_len(int n, LenTables& L) {
   }
   int ntw = 0;
   for (int p = 0; p < L.npass; ++p) ntw += L.ns[p] * L.radix[p];
+  L.ntw = ntw;
   std::vector<double2> tw(ntw);
   for (int p = 0; p < L.npass; ++p) {
     const int R = L.radix[p], Ns = L.ns[p];
@@ -306,10 +333,13 @@ template <> FFTLen<double> LenTables::view<double>() const {
   FFTLen<double> d;
   d.n = n;
   d.npass = npass;
+  d.ntw = ntw;
   for (int i = 0; i < kMaxPass; ++i) {
     d.radix[i] = radix[i];
     d.ns[i] = ns[i];
     d.twoff[i] = twoff[i];
+    d.inv_m[i] = radix[i] ? 1.0f / (float)(n / radix[i]) : 0.f;
+    d.inv_ns[i] = ns[i] ? 1.0f / (float)ns[i] : 0.f;
   }
   d.tw = d_tw64;
   d.gtab = d_g64;
@@ -322,10 +352,13 @@ template <> FFTLen<df32> LenTables::view<df32>() const {
   FFTLen<df32> d;
   d.n = n;
   d.npass = npass;
+  d.ntw = ntw;
   for (int i = 0; i < kMaxPass; ++i) {
     d.radix[i] = radix[i];
     d.ns[i] = ns[i];
     d.twoff[i] = twoff[i];
+    d.inv_m[i] = radix[i] ? 1.0f / (float)(n / radix[i]) : 0.f;
+    d.inv_ns[i] = ns[i] ? 1.0f / (float)ns[i] : 0.f;
   }
   d.tw = d_twdf;
   d.gtab = d_gdf;
@@ -338,10 +371,13 @@ template <> FFTLen<float> LenTables::view<float>() const {
   FFTLen<float> d;
   d.n = n;
   d.npass = npass;
+  d.ntw = ntw;
   for (int i = 0; i < kMaxPass; ++i) {
     d.radix[i] = radix[i];
     d.ns[i] = ns[i];
     d.twoff[i] = twoff[i];
+    d.inv_m[i] = radix[i] ? 1.0f / (float)(n / radix[i]) : 0.f;
+    d.inv_ns[i] = ns[i] ? 1.0f / (float)ns[i] : 0.f;
   }
   d.tw = d_tw32;
   d.gtab = d_g32;

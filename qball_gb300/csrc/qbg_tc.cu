@@ -312,7 +312,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int mt = blockIdx.x, nt = blockIdx.y, z = blockIdx.z;
+  // the N tiles of one M tile are adjacent in launch order, so the A block
+  // (the large projector operand) is fetched from HBM once and re-read from L2
+  const int nt = blockIdx.x, mt = blockIdx.y, z = blockIdx.z;
   const int ks0 = z * args.ks_per_split;
   // a CTA that starts after another one failed does no work
   const int nks = *(volatile const int*)args.status ? 0 : min(args.ks_per_split, args.nKS - ks0);
@@ -597,15 +599,19 @@ qbg_status tc_build(qbg_plan* p, cudaStream_t st) {
 
 static qbg_status tc_launch(qbg_plan* p, int mode, const TcArgs& a, int mt, int nt, int nsplit,
                             cudaStream_t st) {
+  if (mt > 65535 || nsplit > 65535) {
+    set_error("tensor-core GEMM: %d row tiles exceed the grid limit", mt);
+    return QBG_ERR_UNSUPPORTED;
+  }
   const size_t smem = TC_STAGES * TC_STAGE_BYTES + 1024 + 256;
   if (mode == TC_OUT_PARTIAL) {
     QBG_CUDA(cudaFuncSetAttribute(k_tc_gemm<TC_OUT_PARTIAL>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_tc_gemm<TC_OUT_PARTIAL><<<dim3(mt, nt, nsplit), TC_THREADS, smem, st>>>(a);
+    k_tc_gemm<TC_OUT_PARTIAL><<<dim3(nt, mt, nsplit), TC_THREADS, smem, st>>>(a);
   } else {
     QBG_CUDA(cudaFuncSetAttribute(k_tc_gemm<TC_OUT_HPSI>,
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_tc_gemm<TC_OUT_HPSI><<<dim3(mt, nt, nsplit), TC_THREADS, smem, st>>>(a);
+    k_tc_gemm<TC_OUT_HPSI><<<dim3(nt, mt, nsplit), TC_THREADS, smem, st>>>(a);
   }
   QBG_LAUNCHED(p);
   return QBG_OK;
