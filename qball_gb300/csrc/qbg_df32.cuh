@@ -40,12 +40,15 @@ __device__ __forceinline__ df32 operator+(df32 a, df32 b) {
 }
 __device__ __forceinline__ df32 operator-(df32 a) { return df32(-a.hi, -a.lo); }
 __device__ __forceinline__ df32 operator-(df32 a, df32 b) { return a + (-b); }
+// The FMA-exact error of hi*hi plus the two cross terms stays below half an
+// ulp of the product (for normalised inputs), so the pair (p, e) is already
+// normalised to within a rounding and needs no extra renormalisation.
 __device__ __forceinline__ df32 operator*(df32 a, df32 b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);
   e = __fmaf_rn(a.hi, b.lo, e);
   e = __fmaf_rn(a.lo, b.hi, e);
-  return df_renorm(p, e);
+  return df32(p, e);
 }
 __device__ __forceinline__ df32& operator+=(df32& a, df32 b) { return a = a + b; }
 __device__ __forceinline__ df32& operator*=(df32& a, df32 b) { return a = a * b; }

@@ -337,12 +337,6 @@ __device__ cplx<T>* fft_lines(cplx<T>* A, cplx<T>* B, int nlines, int ls,
       case 4: fft_pass<4, S, T>(A, B, nlines, ls, d, p); break;
       case 5: fft_pass<5, S, T>(A, B, nlines, ls, d, p); break;
       case 8: fft_pass<8, S, T>(A, B, nlines, ls, d, p); break;
-      case 16: fft_pass<16, S, T>(A, B, nlines, ls, d, p); break;
-      case 9: fft_pass<9, S, T>(A, B, nlines, ls, d, p); break;
-      case 6: fft_pass<6, S, T>(A, B, nlines, ls, d, p); break;
-      case 10: fft_pass<10, S, T>(A, B, nlines, ls, d, p); break;
-      case 12: fft_pass<12, S, T>(A, B, nlines, ls, d, p); break;
-      case 15: fft_pass<15, S, T>(A, B, nlines, ls, d, p); break;
       case 7: if constexpr (BIGP) fft_pass<7, S, T>(A, B, nlines, ls, d, p); break;
       case 11: if constexpr (BIGP) fft_pass<11, S, T>(A, B, nlines, ls, d, p); break;
       case 13: if constexpr (BIGP) fft_pass<13, S, T>(A, B, nlines, ls, d, p); break;

@@ -192,22 +192,12 @@ bool is_codelet(int r) {
   }
 }
 
-// Two passes when n = R1 * R2 with both codelets (power-of-two first), else
-// the greedy 8/4/2/odd-prime split.
+// Greedy 8/4/2/odd-prime split.  (Two-pass splits with the 9..16-point
+// codelets were measured slower on GB300: the larger codelets raise the
+// register count of every transform kernel and cut its occupancy.)
 bool factorize(int n, LenTables& L) {
   int r[16], np = 0;
-  if (is_codelet(n)) {
-    r[np++] = n;
-  } else {
-    for (int r1 : {16, 8, 4, 2, 12, 10, 9, 6, 15}) {
-      if (n % r1 == 0 && is_codelet(n / r1)) {
-        r[np++] = r1;
-        r[np++] = n / r1;
-        break;
-      }
-    }
-  }
-  if (np == 0) {
+  {
     int m = n;
     while (m % 8 == 0 && m > 1 && np < 16) { r[np++] = 8; m /= 8; }
     if (m % 4 == 0) { r[np++] = 4; m /= 4; }
