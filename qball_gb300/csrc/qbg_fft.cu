@@ -21,6 +21,7 @@
 #include <algorithm>
 
 #include "qbg_internal.h"
+#include "qbg_lanefft.cuh"
 
 namespace qbg {
 
@@ -313,6 +314,78 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
   }
 }
 
+// ------------------------------------------------- lane-group y pass
+// The y pass of the local-potential product with register-resident columns:
+// each group of B lanes owns one column x of a plane (n1 = A*B values), does
+// the backward transform (L1 -> L2), multiplies by v(x, y, z) in the L2
+// layout and transforms forward (L2 -> L1) with no shared-memory round trip
+// or barrier in between.  Shared memory only stages the band-row tile and
+// the v tile so that global accesses stay coalesced.
+constexpr int kLgThreads = 128;
+
+template <typename T, int A, int B>
+__global__ void __launch_bounds__(kLgThreads)
+k_y_lg_vloc(cplx<T>* __restrict__ Y, int nband, int ntrans0, int n0, int n2,
+            const T* __restrict__ v, FFTLen<T> d) {
+  using C = cplx<T>;
+  constexpr int n1 = A * B;
+  constexpr int CPC = (kLgThreads / 32) * (32 / B);  // columns per CTA
+  constexpr int LD = CPC + 1;
+  extern __shared__ __align__(16) unsigned char smem[];
+  C* Wn = reinterpret_cast<C*>(smem);                 // n1 roots
+  C* T_ = Wn + n1;                                    // [nband][LD]
+  T* V = reinterpret_cast<T*>(T_ + (size_t)nband * LD);  // [n1][LD]
+  const int nct = (n0 + CPC - 1) / CPC;
+  const int z = blockIdx.x / nct;
+  const int x0 = (blockIdx.x % nct) * CPC;
+  const int s = blockIdx.y;
+  const int ncol = min(CPC, n0 - x0);
+  C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
+  const T* vz = v + (size_t)z * n0 * n1;
+  for (int i = threadIdx.x; i < n1; i += blockDim.x) Wn[i] = d.root[i];
+  for (int it = threadIdx.x; it < nband * CPC; it += blockDim.x) {
+    const int b = it / CPC, c = it - b * CPC;
+    if (c < ncol) T_[b * LD + c] = Yp[(size_t)b * n0 + x0 + c];
+  }
+  for (int it = threadIdx.x; it < n1 * CPC; it += blockDim.x) {
+    const int y = it / CPC, c = it - y * CPC;
+    if (c < ncol) V[y * LD + c] = vz[(size_t)y * n0 + x0 + c];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int b = lane & (B - 1);
+  const int c = (threadIdx.x >> 5) * (32 / B) + lane / B;
+  const bool live = c < ncol;
+  C r[A];
+#pragma unroll
+  for (int a = 0; a < A; ++a) {
+    const int y = b + B * a;
+    const int bi = y < ntrans0 ? y : (y >= n1 - ntrans0 ? y - n1 + nband : -1);
+    r[a] = (live && bi >= 0) ? T_[bi * LD + c] : cmk<C>(T(0), T(0));
+  }
+  regs_then_lanes<+1, A, B>(r, b, Wn);
+  const int rb = lane_rev<B>(b);
+#pragma unroll
+  for (int a = 0; a < A; ++a) {
+    const T vv = live ? V[(a + A * rb) * LD + c] : T(0);
+    r[a].x = r[a].x * vv;
+    r[a].y = r[a].y * vv;
+  }
+  lanes_then_regs<-1, A, B>(r, b, Wn);
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < A; ++a) {
+    const int y = b + B * a;
+    const int bi = y < ntrans0 ? y : (y >= n1 - ntrans0 ? y - n1 + nband : -1);
+    if (live && bi >= 0) T_[bi * LD + c] = r[a];
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < nband * CPC; it += blockDim.x) {
+    const int bb = it / CPC, cc = it - bb * CPC;
+    if (cc < ncol) Yp[(size_t)bb * n0 + x0 + cc] = T_[bb * LD + cc];
+  }
+}
+
 // ------------------------------------------------------------- launchers
 template <typename T> static size_t smem_bytes(const FFTLen<T>& d) {
   return (2 * (size_t)kTile * (d.n + 1) + d.ntw + kGtab) * sizeof(cplx<T>);
@@ -399,9 +472,65 @@ static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, doubl
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
+template <typename T, int A, int B>
+static qbg_status run_y_lg_vloc(qbg_plan* p, int ns, cudaStream_t st) {
+  const FFTLen<T> d = p->len[1].view<T>();
+  constexpr int CPC = (kLgThreads / 32) * (32 / B);
+  const size_t sm = (size_t)A * B * sizeof(cplx<T>) + (size_t)p->nband * (CPC + 1) * sizeof(cplx<T>) +
+                    (size_t)A * B * (CPC + 1) * sizeof(T);
+  QBG_CUDA(prep(k_y_lg_vloc<T, A, B>, sm));
+  const T* v = std::is_same<T, double>::value  ? (const T*)p->d_vr
+               : std::is_same<T, float>::value ? (const T*)p->d_vr32
+                                               : (const T*)p->d_vrdf;
+  dim3 grid(p->np2 * ((p->np0 + CPC - 1) / CPC), ns);
+  PhaseTimer pt(p, PH_Y_VLOC, st);
+  k_y_lg_vloc<T, A, B><<<grid, kLgThreads, sm, st>>>((cplx<T>*)p->d_Y, p->nband, p->ntrans0,
+                                                     p->np0, p->np2, v, d);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+// lane-group split of the y length, or 0 when the Stockham engine is used
+static int lg_split(int n1) {
+  switch (n1) {
+    case 32: return 4 * 100 + 8;
+    case 48: return 6 * 100 + 8;
+    case 64: return 8 * 100 + 8;
+    case 96: return 12 * 100 + 8;
+    case 120: return 15 * 100 + 8;
+    case 144: return 9 * 100 + 16;
+    case 160: return 10 * 100 + 16;
+    default: return 0;
+  }
+}
+
+template <typename T>
+static qbg_status run_y_vloc(qbg_plan* p, int ns, cudaStream_t st, bool* done) {
+  *done = true;
+  if (!p->lane_fft) {
+    *done = false;
+    return QBG_OK;
+  }
+  switch (lg_split(p->np1)) {
+    case 408: return run_y_lg_vloc<T, 4, 8>(p, ns, st);
+    case 608: return run_y_lg_vloc<T, 6, 8>(p, ns, st);
+    case 808: return run_y_lg_vloc<T, 8, 8>(p, ns, st);
+    case 1208: return run_y_lg_vloc<T, 12, 8>(p, ns, st);
+    case 1508: return run_y_lg_vloc<T, 15, 8>(p, ns, st);
+    case 916: return run_y_lg_vloc<T, 9, 16>(p, ns, st);
+    case 1016: return run_y_lg_vloc<T, 10, 16>(p, ns, st);
+    default: *done = false; return QBG_OK;
+  }
+}
+
 template <typename T, int MODE>
 static qbg_status run_y(qbg_plan* p, int ns, double2* f, const double* w, double* rho,
                         int rho_acc, cudaStream_t st) {
+  if (MODE == Y_VLOC) {
+    bool done = false;
+    qbg_status s = run_y_vloc<T>(p, ns, st, &done);
+    if (done || s != QBG_OK) return s;
+  }
   return big_prime(p->len[1]) ? run_y_<T, MODE, true>(p, ns, f, w, rho, rho_acc, st)
                               : run_y_<T, MODE, false>(p, ns, f, w, rho, rho_acc, st);
 }

@@ -54,6 +54,7 @@ template <typename T> struct FFTLen {
   int ntw;                 // twiddle table length
   const cplx<T>* tw;    // exp(-2 pi i r k / (ns*radix)), k<ns, r<radix
   const cplx<T>* gtab;  // exp(-2 pi i m / p) for the direct-DFT primes
+  const cplx<T>* root;  // exp(-2 pi i m / n), m < n
   int goff7, goff11, goff13;
 };
 

@@ -41,6 +41,9 @@ struct LenTables {
   float2* d_g32 = nullptr;
   df32c* d_twdf = nullptr;
   df32c* d_gdf = nullptr;
+  double2* d_root64 = nullptr;  // exp(-2 pi i m / n), m < n
+  float2* d_root32 = nullptr;
+  df32c* d_rootdf = nullptr;
   template <typename T> FFTLen<T> view() const;
 };
 
@@ -105,6 +108,7 @@ struct qbg_plan {
   bool nl_ready = false;
   void* tc = nullptr;          // tensor-core projector tables (mixed)
   bool check_every_step = true; // read the tensor-core status word after each step
+  bool lane_fft = true;         // register-resident lane-group transforms where supported
   int tc_nst_cleared = 0;
 
   // scratch (allocated lazily, grown as needed)

@@ -282,6 +282,25 @@ qbg_status build_len(int n, LenTables& L) {
         gdf[off[q] + m] = df32c{to_df(std::cos(ang)), to_df(-std::sin(ang))};
       }
   }
+  {
+    std::vector<double2> r64(n);
+    std::vector<float2> r32(n);
+    std::vector<df32c> rdf(n);
+    for (int m = 0; m < n; ++m) {
+      const long double pi = 3.14159265358979323846264338327950288L;
+      const long double ang = 2.0L * pi * (long double)m / (long double)n;
+      const long double c = std::cos(ang), sn = -std::sin(ang);
+      r64[m] = make_double2((double)c, (double)sn);
+      r32[m] = make_float2((float)c, (float)sn);
+      rdf[m] = df32c{to_df(c), to_df(sn)};
+    }
+    QBG_CUDA(cudaMalloc(&L.d_root64, sizeof(double2) * n));
+    QBG_CUDA(cudaMalloc(&L.d_root32, sizeof(float2) * n));
+    QBG_CUDA(cudaMalloc(&L.d_rootdf, sizeof(df32c) * n));
+    QBG_CUDA(cudaMemcpy(L.d_root64, r64.data(), sizeof(double2) * n, cudaMemcpyHostToDevice));
+    QBG_CUDA(cudaMemcpy(L.d_root32, r32.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    QBG_CUDA(cudaMemcpy(L.d_rootdf, rdf.data(), sizeof(df32c) * n, cudaMemcpyHostToDevice));
+  }
   QBG_CUDA(cudaMalloc(&L.d_twdf, sizeof(df32c) * ntw));
   QBG_CUDA(cudaMalloc(&L.d_gdf, sizeof(df32c) * gdf.size()));
   QBG_CUDA(cudaMemcpy(L.d_twdf, twdf.data(), sizeof(df32c) * ntw, cudaMemcpyHostToDevice));
@@ -304,8 +323,14 @@ void free_len(LenTables& L) {
   cudaFree(L.d_g32);
   cudaFree(L.d_twdf);
   cudaFree(L.d_gdf);
+  cudaFree(L.d_root64);
+  cudaFree(L.d_root32);
+  cudaFree(L.d_rootdf);
   L.d_twdf = nullptr;
   L.d_gdf = nullptr;
+  L.d_root64 = nullptr;
+  L.d_root32 = nullptr;
+  L.d_rootdf = nullptr;
   L.d_tw64 = nullptr;
   L.d_tw32 = nullptr;
   L.d_g64 = nullptr;
@@ -333,6 +358,7 @@ template <> FFTLen<double> LenTables::view<double>() const {
   }
   d.tw = d_tw64;
   d.gtab = d_g64;
+  d.root = d_root64;
   d.goff7 = goff7;
   d.goff11 = goff11;
   d.goff13 = goff13;
@@ -352,6 +378,7 @@ template <> FFTLen<df32> LenTables::view<df32>() const {
   }
   d.tw = d_twdf;
   d.gtab = d_gdf;
+  d.root = d_rootdf;
   d.goff7 = goff7;
   d.goff11 = goff11;
   d.goff13 = goff13;
@@ -371,6 +398,7 @@ template <> FFTLen<float> LenTables::view<float>() const {
   }
   d.tw = d_tw32;
   d.gtab = d_g32;
+  d.root = d_root32;
   d.goff7 = goff7;
   d.goff11 = goff11;
   d.goff13 = goff13;

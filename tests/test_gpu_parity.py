@@ -128,6 +128,20 @@ def test_hpsi_fp64_vs_oracle(cuda, name):
     assert np.abs(m - m.conj().T).max() < 1e-10 * np.abs(m).max()
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed_df32", 2e-6)])
+def test_hpsi_216_atom_grid(cuda, prec, tol):
+    """The 120^3 grid and 161 235-wave basis of the 216-atom cell (register
+    lane-group y pass, 15 x 8), with 8 atoms and 4 states to keep the oracle
+    quick."""
+    cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=4)
+    occ = synth.occupations(cell)
+    torch = _torch()
+    out = torch.zeros_like(dev(psi))
+    H.hpsi(dev(psi), out, occ)
+    ref, _ = oh.hpsi(psi.T, occ, nthreads=NT)
+    assert rel_err(out.cpu().numpy(), ref.T) < tol
+
+
 def test_hpsi_pieces_local_only_and_no_states(cuda):
     cell = synth.make_cell("t12b")
     b = Q.Basis(cell.L, cell.ecut)
