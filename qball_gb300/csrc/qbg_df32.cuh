@@ -31,13 +31,20 @@ __device__ __forceinline__ df32 df_renorm(float s, float e) {
   return df32(h, e - (h - s));
 }
 
+// Sum without the final renormalisation: (s, e) with s = fl(a.hi + b.hi),
+// e = exact error of that sum + a.lo + b.lo.  The pair may carry |e| of a
+// few ulp(s) (more after cancellation), but its absolute error stays a few
+// 2^-47 of the operands' magnitude, which is the norm-wise accuracy an FFT
+// needs; every consumer (sum, product, conversion) accepts such pairs.
 __device__ __forceinline__ df32 operator+(df32 a, df32 b) {
   const float s = a.hi + b.hi;
   const float bb = s - a.hi;
   float e = (a.hi - (s - bb)) + (b.hi - bb);
   e += a.lo + b.lo;
-  return df_renorm(s, e);
+  return df32(s, e);
 }
+// exact scaling by a power of two
+__host__ __device__ __forceinline__ df32 df_scale2(df32 a, float p2) { return df32(a.hi * p2, a.lo * p2); }
 __device__ __forceinline__ df32 operator-(df32 a) { return df32(-a.hi, -a.lo); }
 __device__ __forceinline__ df32 operator-(df32 a, df32 b) { return a + (-b); }
 // The FMA-exact error of hi*hi plus the two cross terms stays below half an

@@ -507,7 +507,10 @@ static int lg_split(int n1) {
 template <typename T>
 static qbg_status run_y_vloc(qbg_plan* p, int ns, cudaStream_t st, bool* done) {
   *done = true;
-  if (!p->lane_fft) {
+  // the shuffle network's per-stage twiddles pay off only where the pass is
+  // latency bound (FP32); the FP64 and double-float passes are arithmetic
+  // bound and run faster through the shared-memory radix-8/3/5 engine
+  if (!p->lane_fft || !std::is_same<T, float>::value) {
     *done = false;
     return QBG_OK;
   }

@@ -87,11 +87,18 @@ template <int S, typename C> __host__ __device__ __forceinline__ void dft2(C* v)
   v[1] = csub(a, b);
 }
 
+// x/2 (exact): a plain product for float/double, component scaling for
+// double-float
+template <typename T> __host__ __device__ __forceinline__ T half_of(T x) { return x * T(0.5); }
+template <> __host__ __device__ __forceinline__ df32 half_of<df32>(df32 x) {
+  return df_scale2(x, 0.5f);
+}
+
 template <int S, typename C> __host__ __device__ __forceinline__ void dft3(C* v) {
   using T = decltype(C::x);
   const T h = T(0.86602540378443864676372317075293618);  // sin(2 pi/3)
   C t1 = cadd(v[1], v[2]);
-  C t2 = cmk<C>(v[0].x - T(0.5) * t1.x, v[0].y - T(0.5) * t1.y);
+  C t2 = cmk<C>(v[0].x - half_of(t1.x), v[0].y - half_of(t1.y));
   C d = csub(v[1], v[2]);
   C t3 = cmul_si<S>(cmk<C>(h * d.x, h * d.y));
   v[0] = cadd(v[0], t1);
@@ -135,12 +142,19 @@ template <int S, typename C> __host__ __device__ __forceinline__ void dft8(C* v)
   C o[4] = {v[1], v[3], v[5], v[7]};
   dft4<S>(e);
   dft4<S>(o);
-  // o1 *= (1+Si)/sqrt2, o2 *= S i, o3 *= (-1+Si)/sqrt2
+  // o1 *= (1+Si)/sqrt2, o2 *= S i, o3 *= (-1+Si)/sqrt2 (S = +-1 folded into
+  // the sums, no multiplication by S)
   C x = o[1];
-  o[1] = cmk<C>(r2 * (x.x - T(S) * x.y), r2 * (x.y + T(S) * x.x));
+  if (S > 0)
+    o[1] = cmk<C>(r2 * (x.x - x.y), r2 * (x.y + x.x));
+  else
+    o[1] = cmk<C>(r2 * (x.x + x.y), r2 * (x.y - x.x));
   o[2] = cmul_si<S>(o[2]);
   x = o[3];
-  o[3] = cmk<C>(r2 * (-x.x - T(S) * x.y), r2 * (-x.y + T(S) * x.x));
+  if (S > 0)
+    o[3] = cmk<C>(-(r2 * (x.x + x.y)), r2 * (x.x - x.y));
+  else
+    o[3] = cmk<C>(r2 * (x.y - x.x), -(r2 * (x.x + x.y)));
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     v[k] = cadd(e[k], o[k]);
