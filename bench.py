@@ -8,11 +8,14 @@ of the plain FP64 form (profiles/accuracy.json, produced by python -m
 qball_gb300.accuracy).  The FP32-transform form, the FP64-transform form and
 the plain FP64 form are timed beside it under `other_forms`.
 
-One "step" is one ETRS step of ExponentialWavefunctionStepper (preupdate +
-update: three 4th-order Taylor exponentials = 12 H|psi> applications, plus
-the density of the predicted state) over all 432 states of the synthetic
+One "step" is one ETRS step of EhrenSampleStepper with the
+ExponentialWavefunctionStepper (preupdate + update: three 4th-order Taylor
+exponentials = 12 H|psi> applications) over all 432 states of the synthetic
 216-atom cell (L = 30 bohr, ecut 50 Ry, 120^3 grid, 161 235 full-sphere
-plane waves, 9 KB projectors per atom), delta-kicked by A = (0, 0, 0.01).
+plane waves, 9 KB projectors per atom), delta-kicked by A = (0, 0, 0.01),
+with the self-consistent Hamiltonian (--hxc on, the default): the density of
+psi(t) and of the predicted psi(t+dt) each rebuild v_r = v_ion + v_H + v_xc
+(LDA) on the 135 Ry density sphere that the 120^3 grid holds.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -57,6 +60,8 @@ def parse():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--chunk", type=int, default=0)
+    ap.add_argument("--hxc", default="on", choices=["on", "off"],
+                    help="self-consistent Hartree + LDA potential inside the step")
     ap.add_argument("--form", default="mixed_df32",
                     help="precision form timed for `value` (the fastest form whose 200-step "
                          "dipole error is within 1e-8 of the FP64 form)")
@@ -167,6 +172,25 @@ def make_system(cfg, precision, psi_np=None, chunk=0):
     return cell, basis, H, psi_np
 
 
+def enable_hxc(H, cell, p, occ):
+    """Density basis, ionic terms, v_r of the density of p, and the
+    self-consistent step (EhrenSampleStepper.cc:322-329 before the first
+    step).  Returns the density basis size."""
+    import torch
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    vb = Q.Basis(cell.L, synth.density_ecut(cell))
+    vion, rhopst = synth.ionic_terms(cell, vb)
+    H.set_density_basis(vb)
+    H.set_ionic_terms(vion, rhopst)
+    rho = torch.empty(H.n012, dtype=torch.float64, device=p.device)
+    H.update_density(p, occ, rho)
+    H.update_vhxc(rho)
+    H.set_selfconsistent(True)
+    del rho
+    return vb
+
+
 def make_psi(cell, basis):
     """Seeded random states, Gram-orthonormalised in FP64 on the device."""
     import torch
@@ -263,11 +287,13 @@ def roofline_of(H, cell, basis, prof, peaks):
 
 
 # ------------------------------------------------------------ CPU baseline
-def cpu_baseline(cfg, nsample, reps=1):
+def cpu_baseline(cfg, nsample, reps=1, hxc=True):
     """The CPU oracle (plain-C restatement of the reference path, OpenMP over
     states) on a bounded sample: H|psi> and the density of `nsample` states of
-    the full cell; one ETRS step is extrapolated as 12 H + 1 density over
-    all states (both linear in the number of states)."""
+    the full cell; one ETRS step is extrapolated as 12 H + 2 densities over
+    all states (both linear in the number of states) plus two Hartree + LDA
+    updates of the potential on the full grid (with hxc; else 12 H + 1
+    density)."""
     from oracle import oracle as O
     import qball_gb300 as Q
     from qball_gb300 import synth
@@ -293,11 +319,22 @@ def cpu_baseline(cfg, nsample, reps=1):
     th = np.array(th)
     t_h, t_d = float(th[:, 0].min()), float(th[:, 1].min())
     scale = cell.nst / nsample
-    step_s = (12 * t_h + t_d) * scale
+    t_v = 0.0
+    if hxc:
+        vb = O.Basis(Q.cubic_cell(cell.L), synth.density_ecut(cell))
+        vion, rhopst = synth.ionic_terms(cell, vb)
+        hx = O.Hxc(vb, *cell.grid, vion, rhopst)
+        rho, _ = O.update_density(ft, c, occ, nthreads=cores)
+        t0 = time.perf_counter()
+        hx.update_vhxc(rho)
+        t_v = time.perf_counter() - t0
+    nd = 2 if hxc else 1
+    step_s = (12 * t_h + nd * t_d) * scale + 2 * t_v
+    extra = f" + 2 x Hartree/LDA update ({t_v:.2f} s, 1 thread)" if hxc else ""
     return {"value": 1.0 / step_s, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": (f"oracle H|psi> ({t_h:.2f} s) + density ({t_d:.2f} s) of {nsample} of "
                        f"{cell.nst} states of the full {cfg} cell, {cores} threads; ETRS step "
-                       f"= (12 H + 1 density) x {scale:.0f}")}
+                       f"= (12 H + {nd} density) x {scale:.0f}{extra}")}
 
 
 # ------------------------------------------------------------ arms
@@ -308,7 +345,7 @@ def run_reference(args, rank, world):
     vals = []
     res = None
     for i in range(W + K):
-        res = cpu_baseline(args.config, args.cpu_states)
+        res = cpu_baseline(args.config, args.cpu_states, hxc=args.hxc == "on")
         if i >= W:
             vals.append(res["value"])
     v = float(np.median(vals))
@@ -346,6 +383,8 @@ def run_ours(args, rank, world, local):
     occ = synth.occupations(cell)
     A = synth.kick()
     H.set_vector_potential(A)
+    hxc = args.hxc == "on"
+    vb = enable_hxc(H, cell, psi, occ) if hxc else None
     p = psi.clone()
     barrier(world)
     clocks = Clocks(local)
@@ -402,6 +441,8 @@ def run_ours(args, rank, world, local):
             continue
         _, _, H2, _ = make_system(args.config, form, psi_np=psi)
         H2.set_vector_potential(A)
+        if hxc:
+            enable_hxc(H2, cell, psi, occ)
         p2 = psi.clone()
         ms2, _ = time_etrs(H2, p2, occ, args.dt, A, steps, warm, stream)
         ms2 = allreduce_max(ms2, world)
@@ -417,7 +458,7 @@ def run_ours(args, rank, world, local):
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        cpu = cpu_baseline(args.config, args.cpu_states)
+        cpu = cpu_baseline(args.config, args.cpu_states, hxc=hxc)
 
     if rank == 0:
         form_desc = {
@@ -440,6 +481,11 @@ def run_ours(args, rank, world, local):
                                        f"{cell.grid[0]}^3, {basis.ngw} PW (full sphere), "
                                        f"{cell.nst} states, {nproj_of(cell)} KB projectors, "
                                        f"ETRS dt={args.dt}, delta kick A_z=0.01",
+                           "hamiltonian": (f"self-consistent: v_ion + Hartree + LDA rebuilt from "
+                                           f"the density of psi(t) and of the predicted "
+                                           f"psi(t+dt) every step, density sphere "
+                                           f"{2 * vb.ecut:g} Ry ({vb.ngw} G)" if hxc else
+                                           "fixed local potential"),
                            "l2": "inputs (psi 1.1 GB) larger than L2; no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
                 "gpu_launches": launches, "clocks": clk, "roofline": roofline,

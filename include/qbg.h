@@ -131,6 +131,11 @@ qbg_status qbg_forward(qbg_plan* plan, double* f, double* c, int ldc,
  * with cudaMemcpyDefault). */
 qbg_status qbg_set_vlocal(qbg_plan* plan, const double* v_r);
 
+/* The FP64 local potential in use (EnergyFunctional::v_r, set by
+ * qbg_set_vlocal or rebuilt by qbg_update_vhxc): N doubles to v_r, host or
+ * device (cudaMemcpyDefault); synchronises the device. */
+qbg_status qbg_get_vlocal(const qbg_plan* plan, double* v_r);
+
 /* Kleinman-Bylander projectors of nsp species with the synthetic radial
  * form v_l(g) = g^l exp(-g^2 rc^2/2) (stands in for Species::dvnlg,
  * Species.cc:1492).  All host arrays: na[nsp], lmax[nsp] in {-1,0,1,2},
@@ -175,6 +180,46 @@ qbg_status qbg_density(qbg_plan* plan, const double* psi, int ld, int nst,
 qbg_status qbg_current(qbg_plan* plan, const double* psi, int ld, int nst,
                        const double* occ, double nel, double* J,
                        void* stream);
+
+/* ---- Hartree + exchange-correlation potential -------------------------- */
+/* Density basis of ChargeDensity (ChargeDensity.cc:76-100: the sphere
+ * |G|^2/2 < ecutden, 4 ecut by default) on the plan's grid, for the
+ * transforms of the density and of the local potential (vft).  The basis
+ * must fit the plan's np0 x np1 x np2 grid (FourierTransform.cc:150-200);
+ * the descriptor's kpgx are the G vectors (k = 0). */
+qbg_status qbg_set_density_basis(qbg_plan* plan, const qbg_basis_desc* vbasis);
+
+/* Ionic terms on the density basis: vion_local_g and rhopst of
+ * EnergyFunctional (EnergyFunctional.cc:1895-1915: species' local
+ * pseudopotentials and Gaussian pseudo-charges times structure factors).
+ * Host complex double[2*ngv] each, in the density basis' order; rhopst_g may
+ * be NULL (zero). */
+qbg_status qbg_set_ionic_terms(qbg_plan* plan, const double* vion_g,
+                               const double* rhopst_g);
+
+/* Fourier coefficients of the charge, rhog = forward_v(Omega rho(r))
+ * (ChargeDensity.cc:515-550).  rho: device double[N]; rhog: device complex
+ * double[2*ngv]. */
+qbg_status qbg_density_g(qbg_plan* plan, const double* rho, double* rhog,
+                         void* stream);
+
+/* EnergyFunctional::update_hamiltonian + update_vhxc (EnergyFunctional.cc:
+ * 300-520, TD branch) with the LDA functional (XCPotential::update,
+ * XCPotential.cc:130-190; LDAFunctional::xc_unpolarized, LDAFunctional.cc:
+ * 102-160): from rho (device double[N]) the local potential becomes
+ *   v_r = vxc(rho) + Re backward_v(vion_g + 4 pi (rho_G + rhopst_G) / |G|^2)
+ * with rho_G = forward_v(rho); it replaces what qbg_set_vlocal set.  en
+ * (host double[3], may be NULL) receives {E_H, E_xc, E_ps} (ehart_, exc_,
+ * eps_) and the call then synchronises. */
+qbg_status qbg_update_vhxc(qbg_plan* plan, const double* rho, double* en,
+                           void* stream);
+
+/* on != 0: qbg_etrs_step rebuilds v_r by qbg_update_vhxc from the density of
+ * psi(t) before preupdate (loop top of EhrenSampleStepper::step,
+ * EhrenSampleStepper.cc:322-329) and from the density of the predicted
+ * psi(t+dt) in update() (ExponentialWavefunctionStepper.cc:259-261).  Needs
+ * qbg_set_density_basis and qbg_set_ionic_terms first. */
+qbg_status qbg_set_selfconsistent(qbg_plan* plan, int on);
 
 /* One ETRS step (ExponentialWavefunctionStepper::preupdate + update,
  * ExponentialWavefunctionStepper.cc:153-276; 4th-order Taylor

@@ -72,6 +72,14 @@ def lib():
         L.qbo_current_g.argtypes = [_P, _I, _P, _I, _I, _P, _P, _D, _P]
         L.qbo_etrs_step.argtypes = [_P, _P, _I, _I, _P, _D, _P, _P, _P, _I]
         L.qbo_etrs_step.restype = _D
+        L.qbo_lda.argtypes = [_D, _P, _P]
+        L.qbo_density_g.argtypes = [_P, _P, _D, _P]
+        L.qbo_update_vhxc.argtypes = [_P, _P, _I, _P, _P, _P, _D, _P, _P]
+        L.qbo_update_vhxc.restype = _D
+        L.qbo_etrs_step_hxc.argtypes = [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _I, _P, _P,
+                                        _P, _I]
+        L.qbo_etrs_step_hxc.restype = _D
+        L.qbo_ham_get_vr.argtypes = [_P, _P]
     return _lib
 
 
@@ -95,7 +103,17 @@ def ref():
         R.qbref_ft_destroy.argtypes = [_P]
         R.qbref_ft_backward.argtypes = [_P, _P, _P]
         R.qbref_ft_forward.argtypes = [_P, _P, _P]
+        R.qbref_lda.argtypes = [_I, _P, _P, _P]
     return _ref
+
+
+def ref_lda(rho):
+    """The reference's LDAFunctional::setxc: (exc, vxc) for rho."""
+    rho = np.ascontiguousarray(rho, np.float64)
+    exc = np.zeros_like(rho)
+    vxc = np.zeros_like(rho)
+    ref().qbref_lda(rho.size, _ptr(rho), _ptr(exc), _ptr(vxc))
+    return exc, vxc
 
 
 class Basis:
@@ -279,6 +297,66 @@ class Ham:
         nel = lib().qbo_etrs_step(self.h, _ptr(psi), ngw, nst, _ptr(occ), float(dt),
                                   _ptr(A_t), _ptr(A_tdt), _ptr(rho), nthreads)
         return psi, rho, nel
+
+    def etrs_step_hxc(self, psi, occ, dt, A_t, A_tdt, hxc, want_rho=False, nthreads=1):
+        """ETRS step with v_r rebuilt by update_vhxc (hxc: an Hxc object)."""
+        psi = np.asfortranarray(psi, dtype=np.complex128).copy(order="F")
+        ngw, nst = psi.shape
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        rho = np.zeros(self.ft.n012) if want_rho else None
+        A_t = np.ascontiguousarray(A_t, dtype=np.float64)
+        A_tdt = np.ascontiguousarray(A_tdt, dtype=np.float64)
+        nel = lib().qbo_etrs_step_hxc(self.h, _ptr(psi), ngw, nst, _ptr(occ), float(dt),
+                                      _ptr(A_t), _ptr(A_tdt), hxc.vft.h, _ptr(hxc.vbasis.kpg2),
+                                      hxc.vbasis.ngw, _ptr(hxc.vion), _ptr(hxc.rhopst),
+                                      _ptr(rho), nthreads)
+        return psi, rho, nel
+
+    def v_r_now(self):
+        v = np.zeros(self.ft.n012)
+        lib().qbo_ham_get_vr(self.h, _ptr(v))
+        return v
+
+
+def lda(rho):
+    """(e_xc, v_xc) per grid point, Perdew-Zunger LDA (scalar loop)."""
+    e = ctypes.c_double()
+    v = ctypes.c_double()
+    rho = np.asarray(rho, np.float64).reshape(-1)
+    E = np.zeros_like(rho)
+    V = np.zeros_like(rho)
+    for i, r in enumerate(rho):
+        lib().qbo_lda(float(r), ctypes.byref(e), ctypes.byref(v))
+        E[i] = e.value
+        V[i] = v.value
+    return E, V
+
+
+class Hxc:
+    """Density-basis transform and ionic terms for update_vhxc."""
+
+    def __init__(self, vbasis, np0, np1, np2, vion_g, rhopst_g=None):
+        self.vbasis = vbasis
+        self.vft = FT(vbasis, np0, np1, np2)
+        self.vion = np.ascontiguousarray(np.asarray(vion_g, np.complex128))
+        self.rhopst = (np.ascontiguousarray(np.asarray(rhopst_g, np.complex128))
+                       if rhopst_g is not None else None)
+
+    def density_g(self, rho):
+        rho = np.ascontiguousarray(rho, np.float64)
+        rg = np.zeros(self.vbasis.ngw, np.complex128)
+        lib().qbo_density_g(self.vft.h, _ptr(rho), self.vbasis.omega, _ptr(rg))
+        return rg
+
+    def update_vhxc(self, rho):
+        """(v_r, {ehart, exc, eps})"""
+        rho = np.ascontiguousarray(rho, np.float64)
+        v = np.zeros(self.vft.n012)
+        en = np.zeros(3)
+        lib().qbo_update_vhxc(self.vft.h, _ptr(self.vbasis.kpg2), self.vbasis.ngw,
+                              _ptr(self.vion), _ptr(self.rhopst), _ptr(rho), self.vbasis.omega,
+                              _ptr(v), _ptr(en))
+        return v, dict(zip(("ehart", "exc", "eps"), en.tolist()))
 
 
 def update_density(ft, c, occ, nthreads=1):

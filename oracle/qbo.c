@@ -909,3 +909,130 @@ double qbo_etrs_step(qbo_ham* h, double* psi, int ld, int nst,
   free(newwf);
   return nel;
 }
+
+/* LDA exchange + Perdew-Zunger (1981) parametrisation of the Ceperley-Alder
+ * correlation energy, spin unpolarised, Hartree units -- the functional of
+ * LDAFunctional::xc_unpolarized (functionals/LDAFunctional.cc:102-160).
+ * rs = (3/(4 pi rho))^(1/3); exchange vx = -(3/pi)^(1/3) rho^(1/3) written
+ * through rs; correlation: A ln rs + B + C rs ln rs + D rs for rs < 1,
+ * gamma / (1 + beta1 sqrt(rs) + beta2 rs) otherwise, with C and D fixed by
+ * continuity of e_c and v_c at rs = 1. */
+void qbo_lda(double rh, double* ee, double* vv) {
+  const double c1 = 0.6203504908994001;   /* (3/(4 pi))^(1/3) */
+  const double c3 = -0.610887057711;      /* -(4/3)(3/(4 pi))/(4/(9 pi))^(1/3) */
+  const double A = 0.0311, B = -0.048, b1 = 1.0529, b2 = 0.3334, G = -0.1423;
+  const double D = G / (1.0 + b1 + b2) - B;
+  const double C = -A - D - G * ((b1 / 2.0 + b2) / ((1.0 + b1 + b2) * (1.0 + b1 + b2)));
+  *ee = 0.0;
+  *vv = 0.0;
+  if (rh > 0.0) {
+    const double ro13 = cbrt(rh);
+    const double rs = c1 / ro13;
+    const double vx = c3 / rs, ex = 0.75 * vx;
+    double ec, vc;
+    if (rs < 1.0) {
+      const double logrs = log(rs);
+      ec = A * logrs + B + C * rs * logrs + D * rs;
+      vc = A * logrs + (B - A / 3.0) + (2.0 / 3.0) * C * rs * logrs + ((2.0 * D - C) / 3.0) * rs;
+    } else {
+      const double sqrtrs = sqrt(rs);
+      const double den = 1.0 + b1 * sqrtrs + b2 * rs;
+      ec = G / den;
+      vc = ec * (1.0 + (7.0 / 6.0) * b1 * sqrtrs + (4.0 / 3.0) * b2 * rs) / den;
+    }
+    *ee = ex + ec;
+    *vv = vx + vc;
+  }
+}
+
+void qbo_density_g(const qbo_ft* vft, const double* rho, double omega, double* rhog) {
+  const long n012 = (long)vft->np0 * vft->np1 * vft->np2;
+  double* f = (double*)malloc(sizeof(double) * 2 * (size_t)n012);
+  for (long i = 0; i < n012; ++i) {
+    f[2 * i] = omega * rho[i];
+    f[2 * i + 1] = 0.0;
+  }
+  qbo_ft_forward(vft, f, rhog);
+  free(f);
+}
+
+double qbo_update_vhxc(const qbo_ft* vft, const double* g2, int ngv,
+                       const double* vion_g, const double* rhopst_g,
+                       const double* rho, double omega, double* v_r, double* en) {
+  const long n012 = (long)vft->np0 * vft->np1 * vft->np2;
+  double* f = (double*)malloc(sizeof(double) * 2 * (size_t)n012);
+  double* rg = (double*)malloc(sizeof(double) * 2 * (size_t)(ngv + 1));
+  qbo_density_g(vft, rho, omega, rg);
+  const double omega_inv = 1.0 / omega, fpi = 4.0 * M_PI;
+  double ehsum = 0.0, eps = 0.0;
+  for (int ig = 0; ig < ngv; ++ig) {
+    /* g2i = (1/|G|)^2 (Basis.cc:730-739) */
+    const double g = sqrt(g2[ig]);
+    const double gi = g > 0.0 ? 1.0 / g : 0.0;
+    const double g2i = gi * gi;
+    const double re = omega_inv * rg[2 * ig], im = omega_inv * rg[2 * ig + 1];
+    /* eps: ddot of rhoelg with vion_local_g (EnergyFunctional.cc:456-469) */
+    eps += re * vion_g[2 * ig] + im * vion_g[2 * ig + 1];
+    const double tr = re + (rhopst_g ? rhopst_g[2 * ig] : 0.0);
+    const double ti = im + (rhopst_g ? rhopst_g[2 * ig + 1] : 0.0);
+    ehsum += (tr * tr + ti * ti) * g2i;
+    /* vlocal_g = vion_local_g + 4 pi hamil_rhogt g2i (EnergyFunctional.cc:510-515) */
+    rg[2 * ig] = vion_g[2 * ig] + fpi * tr * g2i;
+    rg[2 * ig + 1] = vion_g[2 * ig + 1] + fpi * ti * g2i;
+  }
+  qbo_ft_backward(vft, rg, f);
+  double exc = 0.0;
+  for (long i = 0; i < n012; ++i) {
+    double e, v;
+    qbo_lda(rho[i], &e, &v);
+    exc += rho[i] * e;
+    v_r[i] = v + f[2 * i];
+  }
+  /* complex basis: vfact 0.5 (EnergyFunctional.cc:494-497) */
+  const double ehart = 0.5 * omega * fpi * ehsum;
+  if (en) {
+    en[0] = ehart;
+    en[1] = exc * omega / (double)n012; /* XCPotential.cc:145-190 */
+    en[2] = eps * omega;
+  }
+  free(f);
+  free(rg);
+  return ehart;
+}
+
+double qbo_etrs_step_hxc(qbo_ham* h, double* psi, int ld, int nst,
+                         const double* occ, double dt, const double* A_t,
+                         const double* A_tdt, const qbo_ft* vft,
+                         const double* g2, int ngv, const double* vion_g,
+                         const double* rhopst_g, double* rho_mid, int nthreads) {
+  const long n012 = (long)h->ft->np0 * h->ft->np1 * h->ft->np2;
+  const size_t len = 2 * (size_t)ld * nst;
+  double* rho = (double*)malloc(sizeof(double) * (size_t)n012);
+  double* dwf = (double*)malloc(sizeof(double) * len);
+  double* expwf = (double*)malloc(sizeof(double) * len);
+  double* newwf = (double*)malloc(sizeof(double) * len);
+  const double dt1 = 0.5 * dt;
+  /* loop top: density of psi(t) and the Hamiltonian built from it */
+  qbo_update_density(h->ft, psi, ld, nst, occ, h->omega, rho, nthreads);
+  qbo_update_vhxc(vft, g2, ngv, vion_g, rhopst_g, rho, h->omega, h->v_r, NULL);
+  qbo_ham_set_A(h, A_t);
+  qbo_exponential(h, psi, ld, nst, occ, dt1, dwf, expwf, nthreads);
+  memcpy(newwf, psi, sizeof(double) * len);
+  qbo_exponential(h, psi, ld, nst, occ, dt1, dwf, expwf, nthreads);
+  const double nel = qbo_update_density(h->ft, psi, ld, nst, occ, h->omega, rho, nthreads);
+  if (rho_mid) memcpy(rho_mid, rho, sizeof(double) * (size_t)n012);
+  qbo_update_vhxc(vft, g2, ngv, vion_g, rhopst_g, rho, h->omega, h->v_r, NULL);
+  qbo_ham_set_A(h, A_tdt);
+  memcpy(psi, newwf, sizeof(double) * len);
+  qbo_exponential(h, psi, ld, nst, occ, dt1, dwf, expwf, nthreads);
+  free(rho);
+  free(dwf);
+  free(expwf);
+  free(newwf);
+  return nel;
+}
+
+void qbo_ham_get_vr(const qbo_ham* h, double* v) {
+  const long n012 = (long)h->ft->np0 * h->ft->np1 * h->ft->np2;
+  memcpy(v, h->v_r, sizeof(double) * (size_t)n012);
+}

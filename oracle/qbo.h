@@ -96,6 +96,23 @@ void qbo_current_g(const double* kpgx, int ngw, const double* c, int ld,
                    int nst, const double* occ, const double* A, double nel,
                    double* J);
 
+/* Hartree + LDA update of the local potential (EnergyFunctional::
+ * update_vhxc, EnergyFunctional.cc:353-520, TD branch; LDA of
+ * LDAFunctional::xc_unpolarized, functionals/LDAFunctional.cc:102-160):
+ *   rho_G = forward_v(omega rho(r)) / omega on the density basis
+ *           (ChargeDensity.cc:515-550, EnergyFunctional.cc:300-323),
+ *   v_r = vxc(rho(r)) + Re backward_v(vion_g + 4 pi (rho_G + rhopst_G) g2i).
+ * vft: transform on the density basis (same grid); g2: its |G|^2 (ngv);
+ * vion_g, rhopst_g: complex [ngv] (rhopst_g may be NULL = zero).
+ * en (may be NULL) receives {E_H, E_xc, E_ps} (ehart_, exc_, eps_). */
+double qbo_update_vhxc(const qbo_ft* vft, const double* g2, int ngv,
+                       const double* vion_g, const double* rhopst_g,
+                       const double* rho, double omega, double* v_r, double* en);
+/* Fourier coefficients of the charge, rhog = forward_v(omega rho(r))
+ * (ChargeDensity.cc:515-550); rhog complex [ngv]. */
+void qbo_density_g(const qbo_ft* vft, const double* rho, double omega, double* rhog);
+void qbo_lda(double rho, double* exc, double* vxc);
+
 /* ETRS step (ExponentialWavefunctionStepper.cc:51-276, order 4, no Hxc
  * feedback): psi advanced in place from t to t+dt.  A_t applies to the
  * first two exponentials, A_tdt to the last one (EhrenSampleStepper.cc:
@@ -104,6 +121,19 @@ void qbo_current_g(const double* kpgx, int ngw, const double* c, int ld,
 double qbo_etrs_step(qbo_ham* h, double* psi, int ld, int nst,
                      const double* occ, double dt, const double* A_t,
                      const double* A_tdt, double* rho_mid, int nthreads);
+
+/* The same step with the self-consistent Hamiltonian: v_r is rebuilt by
+ * qbo_update_vhxc from the density of psi(t) before preupdate (the loop top
+ * of EhrenSampleStepper::step, EhrenSampleStepper.cc:323-329) and from the
+ * density of the predicted psi(t+dt) inside update()
+ * (ExponentialWavefunctionStepper.cc:259-261). */
+double qbo_etrs_step_hxc(qbo_ham* h, double* psi, int ld, int nst,
+                         const double* occ, double dt, const double* A_t,
+                         const double* A_tdt, const qbo_ft* vft,
+                         const double* g2, int ngv, const double* vion_g,
+                         const double* rhopst_g, double* rho_mid, int nthreads);
+
+void qbo_ham_get_vr(const qbo_ham* h, double* v);
 
 #ifdef __cplusplus
 }

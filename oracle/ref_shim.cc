@@ -7,7 +7,9 @@
 #include "Basis.h"
 #include "FourierTransform.h"
 #include "UnitCell.h"
+#include "LDAFunctional.h"
 #include <complex>
+#include <vector>
 
 namespace {
 struct RefBasis {
@@ -85,6 +87,18 @@ void qbref_ft_forward(void* ft, double* f, double* c) {
   static_cast<FourierTransform*>(ft)->forward(
       reinterpret_cast<std::complex<double>*>(f),
       reinterpret_cast<std::complex<double>*>(c));
+}
+
+// LDAFunctional::setxc (functionals/LDAFunctional.cc:39-101), spin
+// unpolarised: exc[i], vxc[i] for rho[i], i < n.
+void qbref_lda(int n, const double* rho, double* exc, double* vxc) {
+  std::vector<std::vector<double> > rhoe(1, std::vector<double>(rho, rho + n));
+  LDAFunctional f(rhoe);
+  f.setxc();
+  for (int i = 0; i < n; ++i) {
+    exc[i] = f.exc[i];
+    vxc[i] = f.vxc1[i];
+  }
 }
 
 }  // extern "C"

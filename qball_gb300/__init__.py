@@ -56,11 +56,17 @@ ABI = {
     "qbg_backward_noalloc": [_P, _P, _I, _P, _I, _P],
     "qbg_forward": [_P, _P, _P, _I, _I, _P],
     "qbg_set_vlocal": [_P, _P],
+    "qbg_get_vlocal": [_P, _P],
     "qbg_set_nonlocal": [_P, _I, _P, _P, _P, _P, _P],
     "qbg_set_vector_potential": [_P, _P],
     "qbg_hpsi": [_P, _P, _I, _P, _I, _P, _P, _P],
     "qbg_density": [_P, _P, _I, _I, _P, _D, _P, _P, _P],
     "qbg_current": [_P, _P, _I, _I, _P, _D, _P, _P],
+    "qbg_set_density_basis": [_P, _P],
+    "qbg_set_ionic_terms": [_P, _P, _P],
+    "qbg_density_g": [_P, _P, _P, _P],
+    "qbg_update_vhxc": [_P, _P, _P, _P],
+    "qbg_set_selfconsistent": [_P, _I],
     "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
     "qbg_launch_count": [_P, _P],
     "qbg_profile": [_P, _I],
@@ -231,6 +237,13 @@ class Hamiltonian(FourierTransform):
         ptr = _np_ptr(v) if isinstance(v, np.ndarray) else _dev_ptr(v)
         _check(lib().qbg_set_vlocal(self.h, ptr), "qbg_set_vlocal")
 
+    def get_vlocal(self, out=None):
+        """The FP64 v_r in use (numpy array, or into the device tensor out)."""
+        v = np.zeros(self.n012) if out is None else out
+        ptr = _np_ptr(v) if isinstance(v, np.ndarray) else _dev_ptr(v)
+        _check(lib().qbg_get_vlocal(self.h, ptr), "qbg_get_vlocal")
+        return v
+
     def set_nonlocal(self, species):
         """species: list of {tau: (na,3), lmax, rc, wt: [w_s, w_p, w_d]}."""
         nsp = len(species)
@@ -246,6 +259,37 @@ class Hamiltonian(FourierTransform):
                if nsp else np.zeros(3))
         _check(lib().qbg_set_nonlocal(self.h, nsp, _np_ptr(na), _np_ptr(lmax), _np_ptr(rc),
                                       _np_ptr(wt), _np_ptr(tau)), "qbg_set_nonlocal")
+
+    # ---- Hartree + xc (EnergyFunctional::update_vhxc)
+    def set_density_basis(self, vbasis):
+        """vbasis: Basis of the density sphere (ecutden, 4 ecut by default) that
+        fits this plan's grid."""
+        d = _BasisDesc(vbasis.ngw, vbasis.nrods, _np_ptr(vbasis.rod_h), _np_ptr(vbasis.rod_k),
+                       _np_ptr(vbasis.rod_lmin), _np_ptr(vbasis.rod_size), _np_ptr(vbasis.kpgx),
+                       vbasis.omega)
+        _check(lib().qbg_set_density_basis(self.h, ctypes.byref(d)), "qbg_set_density_basis")
+        self.vbasis = vbasis
+
+    def set_ionic_terms(self, vion_g, rhopst_g=None):
+        """vion_g, rhopst_g: complex numpy arrays [ngv] on the density basis."""
+        v = np.ascontiguousarray(np.asarray(vion_g, np.complex128).view(np.float64))
+        r = (np.ascontiguousarray(np.asarray(rhopst_g, np.complex128).view(np.float64))
+             if rhopst_g is not None else None)
+        _check(lib().qbg_set_ionic_terms(self.h, _np_ptr(v), _np_ptr(r)), "qbg_set_ionic_terms")
+
+    def density_g(self, rho, rhog, stream=None):
+        _check(lib().qbg_density_g(self.h, _dev_ptr(rho), _dev_ptr(rhog), _stream_ptr(stream)),
+               "qbg_density_g")
+
+    def update_vhxc(self, rho, want_energies=False, stream=None):
+        """Returns {ehart, exc, eps} when want_energies."""
+        en = np.zeros(3)
+        _check(lib().qbg_update_vhxc(self.h, _dev_ptr(rho), _np_ptr(en) if want_energies else None,
+                                     _stream_ptr(stream)), "qbg_update_vhxc")
+        return dict(zip(("ehart", "exc", "eps"), en.tolist())) if want_energies else None
+
+    def set_selfconsistent(self, on=True):
+        _check(lib().qbg_set_selfconsistent(self.h, 1 if on else 0), "qbg_set_selfconsistent")
 
     def set_vector_potential(self, A):
         A = np.ascontiguousarray(A, np.float64)

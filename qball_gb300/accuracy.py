@@ -1,6 +1,6 @@
 """Dipole accuracy of the precision forms against the plain FP64 form.
 
-    python -m qball_gb300.accuracy --config c2 --nst 32 --steps 200
+    python -m qball_gb300.accuracy --config c2 --nst 32 --steps 200 [--hxc on|off]
 
 Propagates the same delta-kicked state with each precision form through the
 C ABI and records the total electronic current J(t) after every ETRS step
@@ -21,16 +21,19 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
 
-def run_form(precision, cell, basis, psi0, occ, A, dt, steps, chunk=0):
+def run_form(precision, cell, basis, psi0, occ, A, dt, steps, chunk=0, hxc=True):
     import torch
     import qball_gb300 as Q
     from qball_gb300 import synth
+    from bench import enable_hxc
     H = Q.Hamiltonian(basis, *cell.grid, precision=precision)
     if chunk:
         H.set_chunk(chunk)
     H.set_vlocal(synth.vlocal(cell))
     H.set_nonlocal(synth.species(cell))
     H.set_vector_potential(A)
+    if hxc:
+        enable_hxc(H, cell, psi0, occ)
     p = psi0.clone()
     nel = float(occ.sum())
     J = [H.current(p, occ, nel)]
@@ -63,6 +66,8 @@ def main():
     ap.add_argument("--forms", default="fp64,mixed")
     ap.add_argument("--out", default="")
     ap.add_argument("--ref", default="", help="npz of an earlier run: reuse its fp64 d(t)")
+    ap.add_argument("--hxc", default="on", choices=["on", "off"],
+                    help="self-consistent Hartree + LDA potential (as bench.py)")
     args = ap.parse_args()
     kw = {"nst": args.nst} if args.nst else {}
     cell = synth.make_cell(args.config, **kw)
@@ -72,7 +77,8 @@ def main():
     A = synth.kick()
     res = {}
     for form in args.forms.split(","):
-        res[form] = run_form(form, cell, basis, psi0, occ, A, args.dt, args.steps)
+        res[form] = run_form(form, cell, basis, psi0, occ, A, args.dt, args.steps,
+                             hxc=args.hxc == "on")
     if args.ref:
         z = np.load(args.ref)
         ref = {"d": z["fp64_d"][:args.steps + 1], "J": z["fp64_J"][:args.steps + 1], "psi": None}
@@ -82,6 +88,7 @@ def main():
     scale_z = np.abs(dref[:, 2]).max()
     scale_n = np.linalg.norm(dref, axis=1).max()
     report = {"config": args.config, "nst": cell.nst, "steps": args.steps, "dt": args.dt,
+              "hxc": args.hxc,
               "kick": list(A), "d64_final": list(map(float, dref[-1])), "forms": {}}
     for form, r in res.items():
         dd = r["d"] - dref

@@ -127,6 +127,16 @@ struct qbg_plan {
   // ETRS work buffers
   void* d_w[4] = {nullptr, nullptr, nullptr, nullptr};
   size_t w_bytes[4] = {0, 0, 0, 0};
+  // Hartree + xc update (qbg_hxc.cu)
+  qbg_plan* vplan = nullptr;     // transform on the density basis, same grid
+  double* d_g2i = nullptr;       // [ngv] 1/|G|^2 (0 at G = 0)
+  double2* d_vion = nullptr;     // [ngv] vion_local_g
+  double2* d_rhopst = nullptr;   // [ngv] rhopst (null: zero)
+  double2* d_vg = nullptr;       // [ngv] rho_G, then v_G
+  double2* d_vf = nullptr;       // [N] complex grid
+  double* d_hxc_red = nullptr;   // energy partials [3][kHxcBlocks]
+  bool have_ionic = false;
+  bool selfconsistent = false;
 };
 
 namespace qbg {
@@ -203,5 +213,10 @@ qbg_status tc_check_status(qbg_plan* p);
 
 // misc kernels (qbg_ops.cu)
 qbg_status update_kinetic(qbg_plan* p, cudaStream_t st);
+
+// Hartree + xc (qbg_hxc.cu): v_r from rho (device), energies stay on the
+// device until read
+qbg_status vhxc_update(qbg_plan* p, const double* rho, cudaStream_t st);
+void hxc_release(qbg_plan* p);
 
 }  // namespace qbg

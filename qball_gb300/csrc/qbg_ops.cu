@@ -201,6 +201,20 @@ qbg_status qbg_set_vlocal(qbg_plan* p, const double* v_r) {
   return QBG_OK;
 }
 
+qbg_status qbg_get_vlocal(const qbg_plan* p, double* v_r) {
+  if (!p || !v_r) {
+    set_error("qbg_get_vlocal: null argument");
+    return QBG_ERR_INVALID;
+  }
+  if (!p->have_vr) {
+    set_error("qbg_get_vlocal: no local potential set");
+    return QBG_ERR_STATE;
+  }
+  QBG_CUDA(cudaDeviceSynchronize());
+  QBG_CUDA(cudaMemcpy(v_r, p->d_vr, sizeof(double) * p->N, cudaMemcpyDefault));
+  return QBG_OK;
+}
+
 qbg_status qbg_set_nonlocal(qbg_plan* p, int nsp, const int* na, const int* lmax,
                             const double* rc, const double* wt, const double* tau) {
   if (!p || nsp < 0 || (nsp > 0 && (!na || !lmax || !rc || !wt))) {
@@ -393,6 +407,16 @@ qbg_status qbg_etrs_step(qbg_plan* p, double* psi_, int ld, int nst, const doubl
   double* d_occ = nullptr;
   QBG_TRY(upload_occ(p, occ, nst, 1.0 / p->omega, &d_occ, st));
   const double dt1 = 0.5 * dt;
+  double* rho = rho_mid;
+  if (!rho || p->selfconsistent) {
+    QBG_TRY(ensure((void**)&p->d_rho, &p->rho_bytes, sizeof(double) * (size_t)p->N));
+    if (!rho) rho = p->d_rho;
+  }
+  if (p->selfconsistent) {
+    // loop top: H(t) from the density of psi(t) (EhrenSampleStepper.cc:322-329)
+    QBG_TRY(density_any(p, psi, ld, nst, d_occ, p->d_rho, st));
+    QBG_TRY(vhxc_update(p, p->d_rho, st));
+  }
   // preupdate: psi(t) -> psi(t+dt/2) (kept), -> predicted psi(t+dt) in X
   QBG_TRY(exponential(p, psi, ld, nst, d_occ, dt1, st));
   const size_t n64 = sizeof(double2) * (size_t)ld * nst;
@@ -406,12 +430,8 @@ qbg_status qbg_etrs_step(qbg_plan* p, double* psi_, int ld, int nst, const doubl
   QBG_TRY(exponential(p, X, ld, nst, d_occ, dt1, st));
   // update: density of the predicted state (hamil_cd()->update_density),
   // then H(t+dt) and the last half step from psi(t+dt/2)
-  double* rho = rho_mid;
-  if (!rho) {
-    QBG_TRY(ensure((void**)&p->d_rho, &p->rho_bytes, sizeof(double) * (size_t)p->N));
-    rho = p->d_rho;
-  }
   QBG_TRY(density_any(p, X, ld, nst, d_occ, rho, st));
+  if (p->selfconsistent) QBG_TRY(vhxc_update(p, rho, st));
   if (nel) {
     double s;
     QBG_TRY(sum_device(p, rho, p->N, &s, st));

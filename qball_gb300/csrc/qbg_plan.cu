@@ -466,6 +466,7 @@ qbg_status qbg_basis_fill(const double* a, double ecut, int* rod_h, int* rod_k,
 qbg_status qbg_plan_destroy(qbg_plan* p) {
   if (!p) return QBG_OK;
   tc_release(p);
+  hxc_release(p);
   for (auto& L : p->len) free_len(L);
   void* bufs[] = {p->d_rods, p->d_row_ptr, p->d_row_rod, p->d_row_x, p->d_band_y,
                   p->d_kpgx, p->d_kpg2A, p->d_kpg2A32, p->d_vr, p->d_vr32, p->d_vrdf,
@@ -642,7 +643,7 @@ qbg_status qbg_launch_count(const qbg_plan* p, long long* count) {
     set_error("qbg_launch_count: null argument");
     return QBG_ERR_INVALID;
   }
-  *count = p->launches;
+  *count = p->launches + (p->vplan ? p->vplan->launches : 0);
   return QBG_OK;
 }
 

@@ -30,6 +30,8 @@ def main():
     ap.add_argument("--natoms", type=int, default=0)
     ap.add_argument("--steps", type=int, default=0)
     ap.add_argument("--hpsi", type=int, default=0)
+    ap.add_argument("--hxc", default="on", choices=["on", "off"],
+                    help="self-consistent Hartree + LDA potential in the ETRS steps")
     args = ap.parse_args()
     kw = {}
     if args.nst:
@@ -52,6 +54,9 @@ def main():
     occ = np.full(cell.nst, 2.0)
     A = synth.kick()
     H.set_vector_potential(A)
+    if args.hxc == "on":
+        from bench import enable_hxc
+        enable_hxc(H, cell, psi, occ)
     out = torch.zeros_like(psi)
     for _ in range(args.hpsi):
         H.hpsi(psi, out, occ)

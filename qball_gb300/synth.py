@@ -9,8 +9,15 @@ No public dataset is involved: every input is generated from a seed.
     image (the real-space form of a Gaussian local pseudopotential);
   * one KB species, lmax 1 (s,p: 4 projectors/atom) or 2 (s,p,d: 9/atom),
     radial form g^l exp(-g^2 rc^2/2) with rc = 1, weights D_l ~ U[0.5, 2] Ha;
-  * occupations 2 (closed shell).
+  * occupations 2 (closed shell);
+  * for the Hartree + xc update: the density basis of the largest cutoff
+    (4 ecut at most) whose grid, by the reference's rule (ChargeDensity.cc:
+    76-100), fits the cell's grid; vion_local_g the Fourier coefficients of
+    the same Gaussian wells; rhopst Gaussian pseudo-charges -Z exp(-G^2
+    rc^2/4)/Omega per atom (rc = 1 bohr), Z = electrons per atom, so that the
+    cell is neutral.
 """
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -123,3 +130,57 @@ def occupations(cell, nst=None):
 def kick(strength=0.01):
     """velocity-gauge delta kick along z (set vector_potential 0 0 A)."""
     return np.array([0.0, 0.0, strength])
+
+
+def _good(n):
+    """Basis::factorizable (Basis.cc:126-150)."""
+    for p in (11, 7, 5, 3, 3):
+        if n % p == 0:
+            n //= p
+    while n % 2 == 0:
+        n //= 2
+    return n == 1
+
+
+def rule_grid(L, ecut):
+    """Edge of the cubic density grid the reference builds for cutoff ecut
+    (Ha): vbasis np + 2, rounded up to a good size (ChargeDensity.cc:76-100,
+    Basis.cc:560-573)."""
+    hmax = int(0.5 + math.sqrt(2.0 * ecut) / (2.0 * math.pi) * L)
+    n = 2 * hmax + 2
+    while not _good(n):
+        n += 2
+    n += 2
+    while not _good(n):
+        n += 2
+    return n
+
+
+def density_ecut(cell):
+    """Density cutoff (Ha): 4 ecut when the reference's grid for it fits the
+    cell's grid, else the largest cutoff below that (0.25 Ha steps) that does
+    (the ecutden option, ChargeDensity.cc:78-79)."""
+    e = 4.0 * cell.ecut
+    while e > cell.ecut and rule_grid(cell.L, e) > min(cell.grid):
+        e -= 0.25
+    return e
+
+
+def ionic_terms(cell, vbasis, depth=-2.0, width=1.0, rcps=1.0, zv=None):
+    """(vion_local_g, rhopst) [ngv] complex on the density basis.
+
+    vion: coefficients of sum_a depth exp(-|r-tau_a|^2/(2 width^2)) (the wells
+    of vlocal()), (2 pi width^2)^(3/2) depth exp(-G^2 width^2/2) S(G)/Omega;
+    rhopst: -zv exp(-G^2 rcps^2/4) S(G)/Omega; S(G) = sum_a exp(-i G.tau_a).
+    """
+    g = vbasis.kpgx.reshape(3, -1)
+    g2 = vbasis.kpg2
+    if zv is None:
+        zv = 2.0 * cell.nst / max(cell.natoms, 1)
+    S = np.zeros(vbasis.ngw, np.complex128)
+    for t in cell.tau:
+        S += np.exp(-1j * (g[0] * t[0] + g[1] * t[1] + g[2] * t[2]))
+    om = vbasis.omega
+    vion = depth * (2.0 * np.pi * width * width) ** 1.5 * np.exp(-0.5 * g2 * width * width) * S / om
+    rhopst = -zv * np.exp(-0.25 * g2 * rcps * rcps) * S / om
+    return vion, rhopst

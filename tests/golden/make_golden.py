@@ -1,13 +1,16 @@
 """Generate the golden vectors in tests/golden/ from the reference itself.
 
 Runs the reference's own Basis::resize and FourierTransform::backward /
-forward (serial FFT_NOLIB build, compiled from the reference sources into
-oracle/_ref by oracle/build_ref.sh) on seeded inputs and stores the results.
+forward (serial FFT_NOLIB build) and LDAFunctional::setxc, compiled from the
+reference sources into oracle/_ref by oracle/build_ref.sh, on seeded inputs
+and stores the results.
 The reference's tests pin nothing on this path, so these files are the pins
 for the oracle restatement (oracle/qbo.c) and for the product's basis
 builder.  Usage:
 
-    sh oracle/build_ref.sh && python tests/golden/make_golden.py
+    sh oracle/build_ref.sh && python tests/golden/make_golden.py [name ...]
+
+(names: the CASES below and "lda"; all when none is given)
 """
 import os
 import sys
@@ -44,10 +47,34 @@ def case_inputs(b, seed=20260):
     return c1, c2
 
 
-def main():
+def lda_densities():
+    """Densities spanning both branches of the correlation fit (rs < 1 and
+    rs >= 1, rs = 1 at rho = 3/(4 pi)), zero and negative values."""
+    rng = np.random.default_rng(11)
+    rs1 = 3.0 / (4.0 * np.pi)
+    return np.concatenate([
+        [0.0, -1e-3, -1.0, 1e-300],
+        np.logspace(-14, 4, 361),
+        rs1 * (1.0 + np.linspace(-1e-6, 1e-6, 21)),
+        rng.uniform(0.0, 0.2, 200),
+    ])
+
+
+def make_lda():
+    rho = lda_densities()
+    exc, vxc = O.ref_lda(rho)
+    np.savez_compressed(os.path.join(HERE, "ref_lda.npz"), rho=rho, exc=exc, vxc=vxc)
+    print("lda", rho.size)
+
+
+def main(names=None):
     if O.ref() is None:
         raise SystemExit("oracle/_ref/libqbref.so is not built (run oracle/build_ref.sh)")
+    if not names or "lda" in names:
+        make_lda()
     for name, L, ecut, grid in CASES:
+        if names and name not in names:
+            continue
         a = np.diag([L, L, L]).reshape(9)
         b = O.Basis(a, ecut, use_ref=True)
         out = dict(a=a, ecut=np.float64(ecut), ngw=b.ngw, nrods=b.nrods,
@@ -74,4 +101,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])
