@@ -28,6 +28,23 @@ namespace qbg {
 constexpr int kTile = 16;     // lines per CTA
 constexpr int kThreads = 256;
 
+// shared-memory elements (complex T) ahead of any v tile: one line buffer
+// when the prime-factor transform runs in place, else two plus the twiddles
+template <typename T>
+__host__ __device__ __forceinline__ int fft_smem_elems(const FFTLen<T>& d, int threads) {
+  const int ls = d.n + 1;
+  if (d.pfa && kTile * d.pfa <= threads) return kTile * ls;
+  return 2 * kTile * ls + d.ntw + kGtab;
+}
+
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src), "n"(BYTES));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 template <typename T> __device__ __forceinline__ cplx<T> czero() {
   cplx<T> c;
   c.x = T(0);
@@ -209,7 +226,6 @@ k_x_fwd(const cplx<T>* __restrict__ Y, cplx<T>* __restrict__ Z, int nrods,
 
 // ------------------------------------------------------------------ y pass
 enum YMode { Y_VLOC = 0, Y_BWD_STORE = 1, Y_FWD_LOAD = 2, Y_DENSITY = 3 };
-constexpr int kDensRegs = 16;  // kTile * n1 / kThreads for n1 <= 256
 
 template <typename T, int MODE, bool BIGP>
 __global__ void __launch_bounds__(kThreads)
@@ -228,12 +244,18 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
   const int x0 = (blockIdx.x % nct) * kTile;
   const int nl = min(kTile, n0 - x0);
   const size_t plane = (size_t)n0 * n1;
-  double dacc[kDensRegs];
-#pragma unroll
-  for (int k = 0; k < kDensRegs; ++k) dacc[k] = 0.0;
-  const int s_begin = MODE == Y_DENSITY ? 0 : blockIdx.y;
-  const int s_end = MODE == Y_DENSITY ? nstates : blockIdx.y + 1;
-  for (int s = s_begin; s < s_end; ++s) {
+  // v tile [n1][kTile], fetched asynchronously during the backward transform
+  T* V = reinterpret_cast<T*>(A + fft_smem_elems(d, blockDim.x));
+  if (MODE == Y_VLOC) {
+    const T* vz = v + (size_t)z * plane;
+    for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
+      const int cl = it % nl, y = it / nl;
+      cp_async<sizeof(T)>(V + y * kTile + cl, vz + (size_t)y * n0 + x0 + cl);
+    }
+    cp_async_commit();
+  }
+  {
+    const int s = blockIdx.y;
     C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
     C* R;
     if (MODE == Y_FWD_LOAD) {
@@ -259,10 +281,11 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
       R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
     }
     if (MODE == Y_VLOC) {
-      const T* vz = v + (size_t)z * plane;
+      // each thread reads back the v elements it fetched itself
+      cp_async_wait_all();
       for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
         const int cl = it % nl, y = it / nl;
-        const T vv = vz[(size_t)y * n0 + x0 + cl];
+        const T vv = V[y * kTile + cl];
         C c = R[cl * ls + y];
         c.x = c.x * vv;
         c.y = c.y * vv;
@@ -280,16 +303,17 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
         fs[(size_t)y * n0 + x0 + cl] = make_double2((double)c.x, (double)c.y);
       }
     } else if (MODE == Y_DENSITY) {
+      // slot s of the density accumulates w_s |psi_s|^2 of this chunk's
+      // state s; every slot element has exactly one writer per launch
       const double ws = w[s];
-#pragma unroll
-      for (int k = 0; k < kDensRegs; ++k) {
-        const int it = threadIdx.x + k * blockDim.x;
-        if (it < nl * n1) {
-          const int cl = it % nl, y = it / nl;
-          const C c = R[cl * ls + y];
-          const double re = (double)c.x, im = (double)c.y;
-          dacc[k] += ws * (re * re + im * im);
-        }
+      double* rz = rho + (size_t)s * plane * n2 + (size_t)z * plane;
+      for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
+        const int cl = it % nl, y = it / nl;
+        const C c = R[cl * ls + y];
+        const double re = (double)c.x, im = (double)c.y;
+        const double a = ws * (re * re + im * im);
+        const size_t idx = (size_t)y * n0 + x0 + cl;
+        rz[idx] = rho_accumulate ? rz[idx] + a : a;
       }
     } else {
       // VLOC, FWD_LOAD: keep the band rows
@@ -298,19 +322,17 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
         Yp[(size_t)b * n0 + x0 + cl] = R[cl * ls + band_y[b]];
       }
     }
-    __syncthreads();
   }
-  if (MODE == Y_DENSITY) {
-    double* rz = rho + (size_t)z * plane;
-#pragma unroll
-    for (int k = 0; k < kDensRegs; ++k) {
-      const int it = threadIdx.x + k * blockDim.x;
-      if (it < nl * n1) {
-        const int cl = it % nl, y = it / nl;
-        const size_t idx = (size_t)y * n0 + x0 + cl;
-        rz[idx] = rho_accumulate ? rz[idx] + dacc[k] : dacc[k];
-      }
-    }
+}
+
+// rho[i] = sum_k slot[k][i] in slot order (deterministic)
+__global__ void __launch_bounds__(256)
+k_sum_slots(const double* __restrict__ slots, int nslots, long long n, double* __restrict__ rho) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    double a = slots[i];
+    for (int k = 1; k < nslots; ++k) a += slots[(size_t)k * n + i];
+    rho[i] = a;
   }
 }
 
@@ -387,8 +409,14 @@ k_y_lg_vloc(cplx<T>* __restrict__ Y, int nband, int ntrans0, int n0, int n2,
 }
 
 // ------------------------------------------------------------- launchers
-template <typename T> static size_t smem_bytes(const FFTLen<T>& d) {
-  return (2 * (size_t)kTile * (d.n + 1) + d.ntw + kGtab) * sizeof(cplx<T>);
+// threads per CTA: the prime-factor passes of a 16-line tile have 15 and 8
+// items per line (120 = 8 x 15), so 128 threads keep both passes busy and
+// leave room for more resident CTAs; the Stockham passes use 256
+template <typename T> static int nthreads(const FFTLen<T>& d) { return d.pfa ? 128 : kThreads; }
+
+template <typename T> static size_t smem_bytes(const FFTLen<T>& d, bool vtile = false) {
+  return (size_t)fft_smem_elems(d, nthreads(d)) * sizeof(cplx<T>) +
+         (vtile ? (size_t)d.n * kTile * sizeof(T) : 0);
 }
 
 template <typename K> static cudaError_t prep(K kernel, size_t smem) {
@@ -418,7 +446,7 @@ static qbg_status run_z_bwd_(qbg_plan* p, const double2* c, int ldc, int ns, cud
   QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   PhaseTimer pt(p, PH_Z_BWD, st);
-  k_z_bwd<T, BIGP><<<grid, kThreads, sm, st>>>(c, ldc, (cplx<T>*)p->d_Z, p->d_rods, p->nrods, d);
+  k_z_bwd<T, BIGP><<<grid, nthreads(d), sm, st>>>(c, ldc, (cplx<T>*)p->d_Z, p->d_rods, p->nrods, d);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
@@ -436,12 +464,12 @@ static qbg_status run_x_(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
   PhaseTimer pt(p, bwd ? PH_X_BWD : PH_X_FWD, st);
   if (bwd) {
     QBG_CUDA(prep(k_x_bwd<T, BIGP>, sm));
-    k_x_bwd<T, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Z, (cplx<T>*)p->d_Y, p->nrods,
+    k_x_bwd<T, BIGP><<<grid, nthreads(d), sm, st>>>((const cplx<T>*)p->d_Z, (cplx<T>*)p->d_Y, p->nrods,
                                            p->nband, p->np2, p->d_row_ptr, p->d_row_rod,
                                            p->d_row_x, d);
   } else {
     QBG_CUDA(prep(k_x_fwd<T, BIGP>, sm));
-    k_x_fwd<T, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Y, (cplx<T>*)p->d_Z, p->nrods,
+    k_x_fwd<T, BIGP><<<grid, nthreads(d), sm, st>>>((const cplx<T>*)p->d_Y, (cplx<T>*)p->d_Z, p->nrods,
                                            p->nband, p->np2, p->d_row_ptr, p->d_row_rod,
                                            p->d_row_x, d);
   }
@@ -457,9 +485,9 @@ template <typename T, int MODE, bool BIGP>
 static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, double* rho,
                          int rho_acc, cudaStream_t st) {
   const FFTLen<T> d = p->len[1].view<T>();
-  const size_t sm = smem_bytes<T>(d);
+  const size_t sm = smem_bytes<T>(d, MODE == Y_VLOC);
   QBG_CUDA(prep(k_y<T, MODE, BIGP>, sm));
-  dim3 grid(p->np2 * ((p->np0 + kTile - 1) / kTile), MODE == Y_DENSITY ? 1 : ns);
+  dim3 grid(p->np2 * ((p->np0 + kTile - 1) / kTile), ns);
   PhaseTimer pt(p, MODE == Y_VLOC ? PH_Y_VLOC : MODE == Y_DENSITY ? PH_Y_DENSITY
                    : MODE == Y_BWD_STORE ? PH_Y_STORE : PH_Y_LOAD, st);
   const T* v = nullptr;
@@ -467,7 +495,7 @@ static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, doubl
     v = std::is_same<T, double>::value  ? (const T*)p->d_vr
         : std::is_same<T, float>::value ? (const T*)p->d_vr32
                                         : (const T*)p->d_vrdf;
-  k_y<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((cplx<T>*)p->d_Y, p->nband, p->np0, p->np2,
+  k_y<T, MODE, BIGP><<<grid, nthreads(d), sm, st>>>((cplx<T>*)p->d_Y, p->nband, p->np0, p->np2,
                                                 p->d_band_y, v, f, w, ns, rho, rho_acc, d);
   QBG_LAUNCHED(p);
   return QBG_OK;
@@ -549,7 +577,7 @@ static qbg_status run_z_fwd_(qbg_plan* p, double2* out, int ldo, int ns, const d
   const T scale = (T)(1.0 / (double)(p->np0 * p->np1 * p->np2));
   const double* kin = p->d_kpg2A;
   PhaseTimer pt(p, PH_Z_FWD, st);
-  k_z_fwd<T, MODE, BIGP><<<grid, kThreads, sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
+  k_z_fwd<T, MODE, BIGP><<<grid, nthreads(d), sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
                                                     p->d_rods, p->nrods, d, scale, psi, ldp,
                                                     kin, out_init, acc, lda, fac);
   QBG_LAUNCHED(p);
@@ -625,11 +653,20 @@ qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst, const double
     QBG_CUDA(cudaMemsetAsync(rho, 0, sizeof(double) * p->N, st));
     return QBG_OK;
   }
+  // one density slot per state of a chunk (grid-sized), summed at the end
+  QBG_TRY(ensure((void**)&p->d_rho_slots, &p->rho_slots_bytes,
+                 sizeof(double) * (size_t)p->N * ch));
   for (int s0 = 0; s0 < nst; s0 += ch) {
     const int ns = std::min(ch, nst - s0);
     QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ldc, ldc, ns, st));
     QBG_TRY(run_x<T>(p, true, ns, st));
-    QBG_TRY((run_y<T, Y_DENSITY>(p, ns, nullptr, d_w + s0, rho, s0 > 0 ? 1 : 0, st)));
+    QBG_TRY((run_y<T, Y_DENSITY>(p, ns, nullptr, d_w + s0, p->d_rho_slots, s0 > 0 ? 1 : 0,
+                                 st)));
+  }
+  {
+    PhaseTimer pt(p, PH_Y_DENSITY, st);
+    k_sum_slots<<<2 * 152 * 4, 256, 0, st>>>(p->d_rho_slots, ch, p->N, rho);
+    QBG_LAUNCHED(p);
   }
   return QBG_OK;
 }

@@ -56,6 +56,7 @@ template <typename T> struct FFTLen {
   const cplx<T>* gtab;  // exp(-2 pi i m / p) for the direct-DFT primes
   const cplx<T>* root;  // exp(-2 pi i m / n), m < n
   int goff7, goff11, goff13;
+  int pfa;  // non-zero: n = pfa * (n / pfa) runs as a prime-factor transform
 };
 
 constexpr int kGtab = 31;  // 7 + 11 + 13 direct-DFT roots
@@ -71,6 +72,7 @@ __device__ __forceinline__ int fdiv(int a, float inv) {
 // caller synchronises before the first pass.
 template <typename T>
 __device__ __forceinline__ FFTLen<T> stage_twiddles(const FFTLen<T>& d, cplx<T>* dst, bool bigp) {
+  if (d.pfa) return d;  // prime-factor lengths use no twiddle table
   for (int i = threadIdx.x; i < d.ntw; i += blockDim.x) dst[i] = d.tw[i];
   if (bigp)
     for (int i = threadIdx.x; i < kGtab; i += blockDim.x) dst[d.ntw + i] = d.gtab[i];
@@ -287,7 +289,7 @@ template <int S, typename C> __host__ __device__ __forceinline__ void dft12(C* v
 }
 
 template <int R, int S, typename C>
-__device__ __forceinline__ void dft_r(C* v, const C* gtab, int g7, int g11, int g13) {
+__host__ __device__ __forceinline__ void dft_r(C* v, const C* gtab, int g7, int g11, int g13) {
   if constexpr (R == 2) dft2<S>(v);
   else if constexpr (R == 3) dft3<S>(v);
   else if constexpr (R == 4) dft4<S>(v);
@@ -342,9 +344,14 @@ __device__ __forceinline__ void fft_pass(const cplx<T>* __restrict__ src,
 // Returns the buffer that holds the result.  Ends with __syncthreads().
 // BIGP selects the build that also carries the 7/11/13 direct DFTs (their
 // unrolled bodies raise the register count of every kernel that holds them).
+template <int S, typename T> __device__ cplx<T>* pfa_dispatch(cplx<T>*, cplx<T>*, int, int, int);
+
 template <int S, typename T, bool BIGP>
 __device__ cplx<T>* fft_lines(cplx<T>* A, cplx<T>* B, int nlines, int ls,
                               const FFTLen<T>& d) {
+  if constexpr (!BIGP) {
+    if (d.pfa) return pfa_dispatch<S, T>(A, B, nlines, ls, d.n);
+  }
   for (int p = 0; p < d.npass; ++p) {
     switch (d.radix[p]) {
       case 2: fft_pass<2, S, T>(A, B, nlines, ls, d, p); break;
@@ -366,3 +373,5 @@ __device__ cplx<T>* fft_lines(cplx<T>* A, cplx<T>* B, int nlines, int ls,
 }
 
 }  // namespace qbg
+
+#include "qbg_pfa.cuh"

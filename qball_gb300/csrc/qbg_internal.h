@@ -118,6 +118,7 @@ struct qbg_plan {
   void* d_fpart = nullptr; size_t fpart_bytes = 0;   // split-K partials
   double* d_red = nullptr; size_t red_bytes = 0;     // reduction partials
   double* d_rho = nullptr; size_t rho_bytes = 0;     // ETRS density scratch
+  double* d_rho_slots = nullptr; size_t rho_slots_bytes = 0;  // [chunk][N] per-state density
   double* h_red = nullptr; size_t h_red_bytes = 0;   // pinned host copy
   // phase profiler (off unless qbg_profile(plan, 1))
   bool prof = false;

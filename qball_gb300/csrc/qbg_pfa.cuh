@@ -1,0 +1,162 @@
+// qbg_pfa.cuh -- prime-factor (Good-Thomas) transforms of lines whose length
+// splits into two coprime factors, N = N1 * N2, gcd(N1, N2) = 1.
+//
+// With the input map n = (N2 n1 + N1 n2) mod N and the output map
+// k = (K1 k1 + K2 k2) mod N (K1 = 1 mod N1, 0 mod N2; K2 = 0 mod N1,
+// 1 mod N2), exp(2 pi i n k / N) = exp(2 pi i n1 k1 / N1) exp(2 pi i n2 k2 / N2),
+// so the transform is N2 transforms of length N1 followed by N1 of length N2
+// with no twiddle factors between them (Good 1958, Thomas 1963).  Against the
+// three-pass mixed-radix Stockham transform this removes every twiddle
+// product and one shared-memory round trip: 120 = 8 x 15 takes two passes
+// of unrolled register codelets (15 = 3 x 5 is itself prime-factor).
+//
+// Pass 1 works in place on the input slots (each (line, n2) item owns the
+// slots n = N2 n1 + N1 n2); pass 2 reads those slots and writes the result in
+// natural order into the second buffer.  Items are numbered line-fastest so
+// that consecutive threads touch consecutive lines: with an odd line stride
+// every shared-memory access of a warp is free of bank conflicts.
+#pragma once
+// included at the end of qbg_fft_engine.cuh
+
+namespace qbg {
+
+constexpr int pfa_inv(int a, int m) {  // a^-1 mod m, gcd(a, m) = 1
+  int r = 1;
+  while ((a * r) % m != 1) ++r;
+  return r;
+}
+constexpr int pfa_gcd(int a, int b) { return b == 0 ? a : pfa_gcd(b, a % b); }
+
+template <int N1, int N2> struct PfaMap {
+  static_assert(pfa_gcd(N1, N2) == 1, "prime-factor split needs coprime factors");
+  static constexpr int N = N1 * N2;
+  static constexpr int K1 = N2 * pfa_inv(N2 % N1, N1);  // 1 mod N1, 0 mod N2
+  static constexpr int K2 = N1 * pfa_inv(N1 % N2, N2);  // 0 mod N1, 1 mod N2
+};
+
+// pass 1 of one (line, n2) item: length-N1 transform of x[N2 n1 + N1 n2]
+template <int N1, int N2, int S, typename C>
+__host__ __device__ __forceinline__ void pfa_item1(C* line, int n2) {
+  constexpr int N = N1 * N2;
+  const int base = N1 * n2;  // < N
+  C v[N1];
+#pragma unroll
+  for (int a = 0; a < N1; ++a) {
+    int i = base + N2 * a;
+    i = i >= N ? i - N : i;
+    v[a] = line[i];
+  }
+  dft_r<N1, S>(v, (const C*)nullptr, 0, 0, 0);
+#pragma unroll
+  for (int a = 0; a < N1; ++a) {
+    int i = base + N2 * a;
+    i = i >= N ? i - N : i;
+    line[i] = v[a];
+  }
+}
+
+// pass 2 of one (line, k1) item: length-N2 transform over n2 of the pass-1
+// results, written to natural order k = K1 k1 + K2 k2 (mod N)
+template <int N1, int N2, int S, typename C>
+__host__ __device__ __forceinline__ void pfa_item2(const C* src, C* dst, int k1) {
+  using M = PfaMap<N1, N2>;
+  constexpr int N = M::N;
+  const int base = N2 * k1;  // < N
+  C v[N2];
+#pragma unroll
+  for (int b = 0; b < N2; ++b) {
+    int i = base + N1 * b;
+    i = i >= N ? i - N : i;
+    v[b] = src[i];
+  }
+  dft_r<N2, S>(v, (const C*)nullptr, 0, 0, 0);
+  const int obase = (M::K1 * k1) % N;
+#pragma unroll
+  for (int b = 0; b < N2; ++b) {
+    int i = obase + (M::K2 * b) % N;
+    i = i >= N ? i - N : i;
+    dst[i] = v[b];
+  }
+}
+
+// Transform of nlines lines of length N1*N2 held in A (line stride ls).
+// When every pass-2 item has a thread of its own (nlines * N1 <= blockDim.x)
+// the result is left in A (each thread holds its item across a barrier) and
+// B is not touched; otherwise it is left in B.  Ends with __syncthreads().
+template <int N1, int N2, int S, typename T>
+__device__ __forceinline__ cplx<T>* pfa_lines(cplx<T>* A, cplx<T>* B, int nlines, int ls) {
+  using C = cplx<T>;
+  using M = PfaMap<N1, N2>;
+  const int items1 = nlines * N2;
+  for (int it = threadIdx.x; it < items1; it += blockDim.x) {
+    const int n2 = it / nlines;
+    const int line = it - n2 * nlines;
+    pfa_item1<N1, N2, S>(A + line * ls, n2);
+  }
+  __syncthreads();
+  const int items2 = nlines * N1;
+  if (items2 <= (int)blockDim.x) {
+    const bool act = (int)threadIdx.x < items2;
+    const int k1 = threadIdx.x / nlines;
+    C* ln = A + (threadIdx.x - k1 * nlines) * ls;
+    C v[N2];
+    if (act) {
+      const int base = N2 * k1;
+#pragma unroll
+      for (int b = 0; b < N2; ++b) {
+        int i = base + N1 * b;
+        i = i >= M::N ? i - M::N : i;
+        v[b] = ln[i];
+      }
+      dft_r<N2, S>(v, (const C*)nullptr, 0, 0, 0);
+    }
+    __syncthreads();
+    if (act) {
+      const int obase = (M::K1 * k1) % M::N;
+#pragma unroll
+      for (int b = 0; b < N2; ++b) {
+        int i = obase + (M::K2 * b) % M::N;
+        i = i >= M::N ? i - M::N : i;
+        ln[i] = v[b];
+      }
+    }
+    __syncthreads();
+    return A;
+  }
+  for (int it = threadIdx.x; it < items2; it += blockDim.x) {
+    const int k1 = it / nlines;
+    const int line = it - k1 * nlines;
+    pfa_item2<N1, N2, S>(A + line * ls, B + line * ls, k1);
+  }
+  __syncthreads();
+  return B;
+}
+
+// prime-factor split used for length n (0: none; the Stockham engine runs)
+__host__ __device__ inline int pfa_split(int n) {
+  switch (n) {
+    case 120: return 8;   // 8 x 15
+    case 48: return 16;   // 16 x 3
+    case 40: return 8;    // 8 x 5
+    case 72: return 8;    // 8 x 9
+    case 80: return 16;   // 16 x 5
+    case 144: return 16;  // 16 x 9
+    default: return 0;
+  }
+}
+
+// Dispatch on the supported lengths; returns nullptr when n has no split.
+template <int S, typename T>
+__device__ cplx<T>* pfa_dispatch(cplx<T>* A, cplx<T>* B, int nlines, int ls, int n) {
+  switch (n) {
+    case 120: return pfa_lines<8, 15, S, T>(A, B, nlines, ls);
+    case 48: return pfa_lines<16, 3, S, T>(A, B, nlines, ls);
+    case 40: return pfa_lines<8, 5, S, T>(A, B, nlines, ls);
+    case 72: return pfa_lines<8, 9, S, T>(A, B, nlines, ls);
+    case 80: return pfa_lines<16, 5, S, T>(A, B, nlines, ls);
+    case 144: return pfa_lines<16, 9, S, T>(A, B, nlines, ls);
+    default: return nullptr;
+  }
+}
+
+}  // namespace qbg

@@ -71,9 +71,13 @@ def test_fft_backward_forward_vs_reference_golden(cuda, name):
 
 @pytest.mark.parametrize("L,ecut,grid", [(12.0, 10.0, (32, 32, 32)), (12.0, 10.0, (20, 24, 30)),
                                          (20.0, 10.0, (48, 48, 48)), (10.0, 6.0, (28, 28, 28)),
-                                         (10.0, 6.0, (22, 22, 26))])
+                                         (10.0, 6.0, (22, 22, 26)),
+                                         (12.0, 10.0, (120, 48, 40)),
+                                         (12.0, 10.0, (72, 80, 144))])
 def test_fft_vs_oracle_many_grids(cuda, L, ecut, grid):
-    """radix 2,3,4,5,8 plus the direct-DFT primes 7, 11 and 13"""
+    """radix 2,3,4,5,8, the direct-DFT primes 7, 11 and 13, and the
+    prime-factor lengths 120 = 8x15, 48 = 16x3, 40 = 8x5, 72 = 8x9,
+    80 = 16x5, 144 = 16x9"""
     b = Q.Basis(L, ecut)
     ob = O.Basis(b.a, ecut)
     oft = O.FT(ob, *grid)
