@@ -400,8 +400,15 @@ def run_ours(args, rank, world, local):
     H.profile(True)
     H.hpsi(p, hp, occ, stream=stream)
     prof = H.profile_read()
+    # and of one density of all states (the step builds two)
+    rho_t = torch.empty(H.n012, dtype=torch.float64, device=p.device)
+    H.profile(True)
+    H.update_density(p, occ, rho_t, stream=stream)
+    prof_rho = {k: round(v[0], 3) for k, v in H.profile_read().items() if v[1]}
     H.profile(False)
+    del rho_t
     roofline = roofline_of(H, cell, basis, prof, peaks)
+    roofline["phases_ms_per_density"] = prof_rho
 
     # end to end through the public API with host buffers
     e2e = None

@@ -246,7 +246,7 @@ qbg_status qbg_launch_count(const qbg_plan* plan, long long* count);
  * accumulators are reset by every call. */
 qbg_status qbg_profile(qbg_plan* plan, int enable);
 /* ms[i], launches[i] for phases i < n (qbg_phase_name(i) gives the name;
- * there are 12 phases). */
+ * there are 13 phases). */
 qbg_status qbg_profile_read(const qbg_plan* plan, double* ms,
                             long long* launches, int n);
 const char* qbg_phase_name(int phase);

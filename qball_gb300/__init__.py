@@ -73,7 +73,7 @@ ABI = {
     "qbg_profile_read": [_P, _P, _P, _I],
     "qbg_phase_name": [_I],
 }
-NPHASE = 12
+NPHASE = 13
 
 
 class QbgError(RuntimeError):
@@ -184,7 +184,7 @@ class FourierTransform:
         _check(lib().qbg_plan_create(ctypes.byref(d), int(np0), int(np1), int(np2), prec,
                                      ctypes.byref(h)), "qbg_plan_create")
         self.h = h
-        self.chunk = 16 if prec in (QBG_PREC_MIXED, QBG_PREC_MIXED_NL64) else 8  # plan default
+        self.chunk = 32  # plan default
 
     def close(self):
         if getattr(self, "h", None):

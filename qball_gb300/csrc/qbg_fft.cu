@@ -325,14 +325,223 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
   }
 }
 
-// rho[i] = sum_k slot[k][i] in slot order (deterministic)
+// rho[i] = sum_k slot[k][i] in slot order (deterministic), in FP64
+template <typename ST>
 __global__ void __launch_bounds__(256)
-k_sum_slots(const double* __restrict__ slots, int nslots, long long n, double* __restrict__ rho) {
+k_sum_slots(const ST* __restrict__ slots, int nslots, long long n, double* __restrict__ rho) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    double a = slots[i];
-    for (int k = 1; k < nslots; ++k) a += slots[(size_t)k * n + i];
+    double a = (double)slots[i];
+    for (int k = 1; k < nslots; ++k) a += (double)slots[(size_t)k * n + i];
     rho[i] = a;
+  }
+}
+
+// ---------------------------------------------- fused x -> y -> x pass
+// The middle of one H psi transform for one (plane z, state s), all in
+// shared memory: the plane's 2*ntrans0 band rows are filled from the z-pass
+// output (one contiguous row of rods), transformed along x, then processed
+// in groups of G columns -- zero-filled y lines, backward y transform,
+// v(r) product (the v tile fetched with cp.async meanwhile), forward y
+// transform, band rows written back -- and transformed forward along x;
+// the rods go back to the same row of Z.  The Y intermediate of the
+// three-kernel path never leaves the SM.  Needs prime-factor lengths along
+// x and y that run in place, and the band rows plus one column group within
+// one CTA's shared memory.
+constexpr int kXyxThreads = 512;
+
+template <typename T, int X1, int X2, int Y1, int Y2>
+__global__ void __launch_bounds__(kXyxThreads, 1)
+k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const RodInfo* __restrict__ rods, int nband,
+           int n2, const int* __restrict__ band_y, const T* __restrict__ v, int G) {
+  using C = cplx<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int n0 = X1 * X2, n1 = Y1 * Y2, ls0 = n0 + 1, ls1 = n1 + 1;
+  C* Xb = reinterpret_cast<C*>(smem);        // [nband][ls0]
+  C* W = Xb + nband * ls0;                   // [G][ls1]
+  T* V = reinterpret_cast<T*>(W + G * ls1);  // [n1][G]
+  const int z = blockIdx.x, s = blockIdx.y;
+  C* Zr = Z + ((size_t)s * n2 + z) * nrods;
+  const size_t plane = (size_t)n0 * n1;
+  for (int i = threadIdx.x; i < nband * ls0; i += blockDim.x) Xb[i] = czero<T>();
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrods; r += blockDim.x) {
+    const int xb = rods[r].xb;
+    Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[r];
+  }
+  __syncthreads();
+  constexpr int rg = kXyxThreads / X1;  // rows per in-place group
+  for (int b0 = 0; b0 < nband; b0 += rg)
+    pfa_lines<X1, X2, +1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  // y by column groups: fill, backward pass 1, backward pass 2 with the v
+  // product fused into its stores, forward pass 1, forward pass 2 storing
+  // only the band rows, straight into Xb
+  using M = PfaMap<Y1, Y2>;
+  const int nlow = nband / 2 + (nband & 1);  // band rows y < nlow are y = b
+  const T* vz = v + (size_t)z * plane;
+  for (int c0 = 0; c0 < n0; c0 += G) {
+    const int gl = min(G, n0 - c0);
+    for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
+      const int cl = it % gl, y = it / gl;
+      cp_async<sizeof(T)>(V + y * G + cl, vz + (size_t)y * n0 + c0 + cl);
+    }
+    cp_async_commit();
+    for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
+      const int cl = it % gl, y = it / gl;
+      const int b = y < nlow ? y : (y >= n1 - (nband - nlow) ? y - n1 + nband : -1);
+      W[cl * ls1 + y] = b >= 0 ? Xb[b * ls0 + c0 + cl] : czero<T>();
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < gl * Y2; it += blockDim.x) {
+      const int n2i = it / gl;
+      pfa_item1<Y1, Y2, +1>(W + (it - n2i * gl) * ls1, n2i);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    const bool act = (int)threadIdx.x < gl * Y1;
+    const int k1 = threadIdx.x / gl;
+    const int cl2 = threadIdx.x - k1 * gl;
+    C* ln = W + cl2 * ls1;
+    C u[Y2];
+    if (act) {
+#pragma unroll
+      for (int b = 0; b < Y2; ++b) {
+        int i2 = Y2 * k1 + Y1 * b;
+        i2 = i2 >= M::N ? i2 - M::N : i2;
+        u[b] = ln[i2];
+      }
+      dft_r<Y2, +1>(u, (const C*)nullptr, 0, 0, 0);
+    }
+    __syncthreads();
+    if (act) {
+      const int obase = (M::K1 * k1) % M::N;
+#pragma unroll
+      for (int b = 0; b < Y2; ++b) {
+        int y = obase + (M::K2 * b) % M::N;
+        y = y >= M::N ? y - M::N : y;
+        const T vv = V[y * G + cl2];
+        C c = u[b];
+        c.x = c.x * vv;
+        c.y = c.y * vv;
+        ln[y] = c;
+      }
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < gl * Y2; it += blockDim.x) {
+      const int n2i = it / gl;
+      pfa_item1<Y1, Y2, -1>(W + (it - n2i * gl) * ls1, n2i);
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+      for (int b = 0; b < Y2; ++b) {
+        int i2 = Y2 * k1 + Y1 * b;
+        i2 = i2 >= M::N ? i2 - M::N : i2;
+        u[b] = ln[i2];
+      }
+      dft_r<Y2, -1>(u, (const C*)nullptr, 0, 0, 0);
+      const int obase = (M::K1 * k1) % M::N;
+#pragma unroll
+      for (int b = 0; b < Y2; ++b) {
+        int y = obase + (M::K2 * b) % M::N;
+        y = y >= M::N ? y - M::N : y;
+        const int bb = y < nlow ? y : (y >= n1 - (nband - nlow) ? y - n1 + nband : -1);
+        if (bb >= 0) Xb[bb * ls0 + c0 + cl2] = u[b];
+      }
+    }
+    __syncthreads();
+  }
+  for (int b0 = 0; b0 < nband; b0 += rg)
+    pfa_lines<X1, X2, -1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  for (int r = threadIdx.x; r < nrods; r += blockDim.x) {
+    const int xb = rods[r].xb;
+    Zr[r] = Xb[(xb >> 16) * ls0 + (xb & 0xffff)];
+  }
+}
+
+// Fused x -> y pass of the density for one (plane z, state s): band rows as
+// in k_xyx_vloc, x backward, then per column group the backward y transform
+// whose last pass writes w_s |psi(r)|^2 straight to density slot s.
+// Density slots hold T-precision sums: double for FP64 transforms,
+// double-float for double-float ones (|psi|^2 and the running sums then stay
+// on the FP32 pipe; GB300 runs FP64 at 1/72 of the FP32 rate).
+template <typename T> struct SlotOf { using type = double; };
+template <> struct SlotOf<df32> { using type = df32; };
+
+template <typename T, int X1, int X2, int Y1, int Y2>
+__global__ void __launch_bounds__(kXyxThreads, 1)
+k_xy_density(const cplx<T>* __restrict__ Z, int nrods, const RodInfo* __restrict__ rods,
+             int nband, int n2, const double* __restrict__ w,
+             typename SlotOf<T>::type* __restrict__ slots, int accumulate, int G) {
+  using C = cplx<T>;
+  using M = PfaMap<Y1, Y2>;
+  using ST = typename SlotOf<T>::type;
+  extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int n0 = X1 * X2, n1 = Y1 * Y2, ls0 = n0 + 1, ls1 = n1 + 1;
+  C* Xb = reinterpret_cast<C*>(smem);  // [nband][ls0]
+  C* W = Xb + nband * ls0;             // [G][ls1]
+  const int z = blockIdx.x, s = blockIdx.y;
+  const C* Zr = Z + ((size_t)s * n2 + z) * nrods;
+  const size_t plane = (size_t)n0 * n1;
+  ST* rz = slots + (size_t)s * plane * n2 + (size_t)z * plane;
+  const T ws = T(w[s]);
+  for (int i = threadIdx.x; i < nband * ls0; i += blockDim.x) Xb[i] = czero<T>();
+  __syncthreads();
+  for (int r = threadIdx.x; r < nrods; r += blockDim.x) {
+    const int xb = rods[r].xb;
+    Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[r];
+  }
+  __syncthreads();
+  constexpr int rg = kXyxThreads / X1;
+  for (int b0 = 0; b0 < nband; b0 += rg)
+    pfa_lines<X1, X2, +1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  // column groups; when accumulating, the slot tile of the group is fetched
+  // with cp.async into S while the group is filled and transformed
+  ST* S = reinterpret_cast<ST*>(W + G * ls1);  // [n1][G]
+  const int nlow = nband / 2 + (nband & 1);
+  for (int c0 = 0; c0 < n0; c0 += G) {
+    const int gl = min(G, n0 - c0);
+    if (accumulate) {
+      for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
+        const int cl = it % gl, y = it / gl;
+        cp_async<sizeof(ST)>(S + y * G + cl, rz + (size_t)y * n0 + c0 + cl);
+      }
+      cp_async_commit();
+    }
+    for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
+      const int cl = it % gl, y = it / gl;
+      const int b = y < nlow ? y : (y >= n1 - (nband - nlow) ? y - n1 + nband : -1);
+      W[cl * ls1 + y] = b >= 0 ? Xb[b * ls0 + c0 + cl] : czero<T>();
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < gl * Y2; it += blockDim.x) {
+      const int n2i = it / gl;
+      pfa_item1<Y1, Y2, +1>(W + (it - n2i * gl) * ls1, n2i);
+    }
+    if (accumulate) cp_async_wait_all();
+    __syncthreads();
+    if ((int)threadIdx.x < gl * Y1) {
+      const int k1 = threadIdx.x / gl;
+      const int cl2 = threadIdx.x - k1 * gl;
+      const C* ln = W + cl2 * ls1;
+      C u[Y2];
+#pragma unroll
+      for (int b = 0; b < Y2; ++b) {
+        int i2 = Y2 * k1 + Y1 * b;
+        i2 = i2 >= M::N ? i2 - M::N : i2;
+        u[b] = ln[i2];
+      }
+      dft_r<Y2, +1>(u, (const C*)nullptr, 0, 0, 0);
+      const int obase = (M::K1 * k1) % M::N;
+#pragma unroll
+      for (int b = 0; b < Y2; ++b) {
+        int y = obase + (M::K2 * b) % M::N;
+        y = y >= M::N ? y - M::N : y;
+        const T a = ws * (u[b].x * u[b].x + u[b].y * u[b].y);
+        rz[(size_t)y * n0 + c0 + cl2] = accumulate ? S[y * G + cl2] + a : a;
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -412,10 +621,23 @@ k_y_lg_vloc(cplx<T>* __restrict__ Y, int nband, int ntrans0, int n0, int n2,
 // threads per CTA: the prime-factor passes of a 16-line tile have 15 and 8
 // items per line (120 = 8 x 15), so 128 threads keep both passes busy and
 // leave room for more resident CTAs; the Stockham passes use 256
-template <typename T> static int nthreads(const FFTLen<T>& d) { return d.pfa ? 128 : kThreads; }
+#ifndef QBG_PFA_THREADS
+#define QBG_PFA_THREADS 128
+#endif
+#ifndef QBG_PFA_THREADS_Z
+#define QBG_PFA_THREADS_Z 128
+#endif
+template <typename T> static int nthreads(const FFTLen<T>& d) {
+  return d.pfa ? QBG_PFA_THREADS : kThreads;
+}
+// z passes: the sphere gather/scatter epilogue runs one warp per rod
+template <typename T> static int nthreads_z(const FFTLen<T>& d) {
+  return d.pfa ? QBG_PFA_THREADS_Z : kThreads;
+}
 
-template <typename T> static size_t smem_bytes(const FFTLen<T>& d, bool vtile = false) {
-  return (size_t)fft_smem_elems(d, nthreads(d)) * sizeof(cplx<T>) +
+template <typename T> static size_t smem_bytes(const FFTLen<T>& d, bool vtile = false,
+                                               int threads = 0) {
+  return (size_t)fft_smem_elems(d, threads ? threads : nthreads(d)) * sizeof(cplx<T>) +
          (vtile ? (size_t)d.n * kTile * sizeof(T) : 0);
 }
 
@@ -442,11 +664,11 @@ static bool big_prime(const LenTables& L) {
 template <typename T, bool BIGP>
 static qbg_status run_z_bwd_(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st) {
   const FFTLen<T> d = p->len[2].view<T>();
-  const size_t sm = smem_bytes<T>(d);
+  const size_t sm = smem_bytes<T>(d, false, nthreads_z(d));
   QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   PhaseTimer pt(p, PH_Z_BWD, st);
-  k_z_bwd<T, BIGP><<<grid, nthreads(d), sm, st>>>(c, ldc, (cplx<T>*)p->d_Z, p->d_rods, p->nrods, d);
+  k_z_bwd<T, BIGP><<<grid, nthreads_z(d), sm, st>>>(c, ldc, (cplx<T>*)p->d_Z, p->d_rods, p->nrods, d);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
@@ -571,13 +793,13 @@ static qbg_status run_z_fwd_(qbg_plan* p, double2* out, int ldo, int ns, const d
                              int ldp, int out_init, double2* acc, int lda, double2 fac,
                              cudaStream_t st) {
   const FFTLen<T> d = p->len[2].view<T>();
-  const size_t sm = smem_bytes<T>(d);
+  const size_t sm = smem_bytes<T>(d, false, nthreads_z(d));
   QBG_CUDA(prep(k_z_fwd<T, MODE, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   const T scale = (T)(1.0 / (double)(p->np0 * p->np1 * p->np2));
   const double* kin = p->d_kpg2A;
   PhaseTimer pt(p, PH_Z_FWD, st);
-  k_z_fwd<T, MODE, BIGP><<<grid, nthreads(d), sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
+  k_z_fwd<T, MODE, BIGP><<<grid, nthreads_z(d), sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
                                                     p->d_rods, p->nrods, d, scale, psi, ldp,
                                                     kin, out_init, acc, lda, fac);
   QBG_LAUNCHED(p);
@@ -598,17 +820,102 @@ static qbg_status run_z_fwd(qbg_plan* p, double2* out, int ldo, int ns, const do
     if (s_ != QBG_OK) return s_;  \
   } while (0)
 
+template <typename T, int X1, int X2, int Y1, int Y2>
+static qbg_status run_xyx_(qbg_plan* p, int ns, int G, size_t sm, cudaStream_t st) {
+  QBG_CUDA(prep(k_xyx_vloc<T, X1, X2, Y1, Y2>, sm));
+  const T* v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vrdf;
+  PhaseTimer pt(p, PH_XYX_VLOC, st);
+  k_xyx_vloc<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), kXyxThreads, sm, st>>>(
+      (cplx<T>*)p->d_Z, p->nrods, p->d_rods, p->nband, p->np2, p->d_band_y, v, G);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+// (n0, n1) pairs with a compiled fused kernel
+static bool xyx_lengths(int n0, int n1) {
+  return n0 == n1 && (n0 == 120 || n0 == 48 || n0 == 40);
+}
+template <typename T, int X1, int X2, int Y1, int Y2>
+static qbg_status run_xy_density_(qbg_plan* p, int ns, const double* w, int acc, int G,
+                                  size_t sm, cudaStream_t st) {
+  QBG_CUDA(prep(k_xy_density<T, X1, X2, Y1, Y2>, sm));
+  PhaseTimer pt(p, PH_Y_DENSITY, st);
+  k_xy_density<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), kXyxThreads, sm, st>>>(
+      (const cplx<T>*)p->d_Z, p->nrods, p->d_rods, p->nband, p->np2, w,
+      (typename SlotOf<T>::type*)p->d_rho_slots, acc, G);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+template <typename T>
+static qbg_status run_xy_density(qbg_plan* p, int ns, const double* w, int acc, int G,
+                                 size_t sm, cudaStream_t st) {
+  switch (p->np0) {
+    case 120: return run_xy_density_<T, 8, 15, 8, 15>(p, ns, w, acc, G, sm, st);
+    case 48: return run_xy_density_<T, 16, 3, 16, 3>(p, ns, w, acc, G, sm, st);
+    default: return run_xy_density_<T, 8, 5, 8, 5>(p, ns, w, acc, G, sm, st);
+  }
+}
+
+template <typename T>
+static qbg_status run_xyx(qbg_plan* p, int ns, int G, size_t sm, cudaStream_t st) {
+  switch (p->np0) {
+    case 120: return run_xyx_<T, 8, 15, 8, 15>(p, ns, G, sm, st);
+    case 48: return run_xyx_<T, 16, 3, 16, 3>(p, ns, G, sm, st);
+    default: return run_xyx_<T, 8, 5, 8, 5>(p, ns, G, sm, st);
+  }
+}
+
+// Column-group width of the fused x -> y -> x kernel, 0 when it does not
+// apply (lengths without an in-place prime-factor split, or shared memory).
+template <typename T> static int xyx_group(const qbg_plan* p, size_t* smem) {
+  const FFTLen<T> dx = p->len[0].view<T>(), dy = p->len[1].view<T>();
+  if (!p->fuse_xyx || !xyx_lengths(p->np0, p->np1) || std::is_same<T, float>::value) return 0;
+  const size_t cs = sizeof(cplx<T>);
+  const size_t base = (size_t)p->nband * (p->np0 + 1) * cs;
+  const size_t per_col = (size_t)(p->np1 + 1) * cs + (size_t)p->np1 * sizeof(T);
+  const size_t cap = 227 * 1024;
+  if (base + per_col > cap || kXyxThreads / dx.pfa < 1) return 0;
+  const int gmax = std::min<int>({(int)((cap - base) / per_col), kXyxThreads / dy.pfa, p->np0});
+  if (gmax < 8) return 0;
+  const int ngroups = (p->np0 + gmax - 1) / gmax;
+  const int G = (p->np0 + ngroups - 1) / ngroups;
+  *smem = base + (size_t)G * per_col;
+  return G;
+}
+
+// Column-group width of the fused density kernel (0: not applicable).
+template <typename T> static int xy_density_group(const qbg_plan* p, size_t* smem) {
+  if (!p->fuse_xyx || !xyx_lengths(p->np0, p->np1) || std::is_same<T, float>::value) return 0;
+  const FFTLen<T> dy = p->len[1].view<T>();
+  const size_t cs = sizeof(cplx<T>);
+  const size_t base = (size_t)p->nband * (p->np0 + 1) * cs;
+  const size_t per_col = (size_t)(p->np1 + 1) * cs + (size_t)p->np1 * sizeof(double);
+  const size_t cap = 227 * 1024;
+  if (base + per_col > cap) return 0;
+  const int gmax = std::min<int>({(int)((cap - base) / per_col), kXyxThreads / dy.pfa, p->np0});
+  if (gmax < 8) return 0;
+  const int ngroups = (p->np0 + gmax - 1) / gmax;
+  const int G = (p->np0 + ngroups - 1) / ngroups;
+  *smem = base + (size_t)G * per_col;
+  return G;
+}
+
 template <typename T>
 qbg_status local_hpsi(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
                       bool out_init, double2* acc, int ldacc, double2 fac, cudaStream_t st) {
   const int ch = std::max(1, std::min(p->chunk, nst));
   QBG_TRY(ensure_scratch<T>(p, ch));
+  size_t xyx_smem = 0;
+  const int G = xyx_group<T>(p, &xyx_smem);
   for (int s0 = 0; s0 < nst; s0 += ch) {
     const int ns = std::min(ch, nst - s0);
     QBG_TRY(run_z_bwd<T>(p, psi + (size_t)s0 * ld, ld, ns, st));
-    QBG_TRY(run_x<T>(p, true, ns, st));
-    QBG_TRY((run_y<T, Y_VLOC>(p, ns, nullptr, nullptr, nullptr, 0, st)));
-    QBG_TRY(run_x<T>(p, false, ns, st));
+    if (G) {
+      if constexpr (!std::is_same<T, float>::value) QBG_TRY(run_xyx<T>(p, ns, G, xyx_smem, st));
+    } else {
+      QBG_TRY(run_x<T>(p, true, ns, st));
+      QBG_TRY((run_y<T, Y_VLOC>(p, ns, nullptr, nullptr, nullptr, 0, st)));
+      QBG_TRY(run_x<T>(p, false, ns, st));
+    }
     QBG_TRY((run_z_fwd<T, 1>(p, out + (size_t)s0 * ld, ld, ns, psi + (size_t)s0 * ld, ld,
                              out_init ? 1 : 0, acc ? acc + (size_t)s0 * ldacc : nullptr, ldacc,
                              fac, st)));
@@ -656,16 +963,26 @@ qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst, const double
   // one density slot per state of a chunk (grid-sized), summed at the end
   QBG_TRY(ensure((void**)&p->d_rho_slots, &p->rho_slots_bytes,
                  sizeof(double) * (size_t)p->N * ch));
+  size_t xy_smem = 0;
+  const int G = xy_density_group<T>(p, &xy_smem);
   for (int s0 = 0; s0 < nst; s0 += ch) {
     const int ns = std::min(ch, nst - s0);
     QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ldc, ldc, ns, st));
-    QBG_TRY(run_x<T>(p, true, ns, st));
-    QBG_TRY((run_y<T, Y_DENSITY>(p, ns, nullptr, d_w + s0, p->d_rho_slots, s0 > 0 ? 1 : 0,
-                                 st)));
+    if (G) {
+      if constexpr (!std::is_same<T, float>::value)
+        QBG_TRY(run_xy_density<T>(p, ns, d_w + s0, s0 > 0 ? 1 : 0, G, xy_smem, st));
+    } else {
+      QBG_TRY(run_x<T>(p, true, ns, st));
+      QBG_TRY((run_y<T, Y_DENSITY>(p, ns, nullptr, d_w + s0, p->d_rho_slots, s0 > 0 ? 1 : 0,
+                                   st)));
+    }
   }
   {
     PhaseTimer pt(p, PH_Y_DENSITY, st);
-    k_sum_slots<<<2 * 152 * 4, 256, 0, st>>>(p->d_rho_slots, ch, p->N, rho);
+    if (G && std::is_same<T, df32>::value)
+      k_sum_slots<df32><<<2 * 152 * 4, 256, 0, st>>>((const df32*)p->d_rho_slots, ch, p->N, rho);
+    else
+      k_sum_slots<double><<<2 * 152 * 4, 256, 0, st>>>(p->d_rho_slots, ch, p->N, rho);
     QBG_LAUNCHED(p);
   }
   return QBG_OK;

@@ -51,7 +51,7 @@ struct LenTables {
 // "fnl_gemm", "enl_hpsi" in NonLocalPotential.cc:2059-2170).
 enum Phase {
   PH_FNL_GEMM = 0, PH_FNL_REDUCE, PH_ENL_HPSI, PH_Z_BWD, PH_X_BWD, PH_Y_VLOC,
-  PH_X_FWD, PH_Z_FWD, PH_Y_DENSITY, PH_Y_STORE, PH_Y_LOAD, PH_MISC, PH_COUNT
+  PH_X_FWD, PH_Z_FWD, PH_Y_DENSITY, PH_Y_STORE, PH_Y_LOAD, PH_MISC, PH_XYX_VLOC, PH_COUNT
 };
 extern const char* const kPhaseName[PH_COUNT];
 
@@ -109,6 +109,7 @@ struct qbg_plan {
   void* tc = nullptr;          // tensor-core projector tables (mixed)
   bool check_every_step = true; // read the tensor-core status word after each step
   bool lane_fft = true;         // register-resident lane-group transforms where supported
+  bool fuse_xyx = true;         // x, y and x passes of H psi in one kernel where they fit
   int tc_nst_cleared = 0;
 
   // scratch (allocated lazily, grown as needed)

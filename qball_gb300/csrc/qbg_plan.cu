@@ -16,7 +16,7 @@ static thread_local std::string g_err;
 
 const char* const kPhaseName[PH_COUNT] = {
     "fnl_gemm", "fnl_reduce", "enl_hpsi", "ft_z_bwd", "ft_x_bwd", "ft_y_vloc",
-    "ft_x_fwd", "ft_z_fwd", "ft_y_density", "ft_y_store", "ft_y_load", "misc"};
+    "ft_x_fwd", "ft_z_fwd", "ft_y_density", "ft_y_store", "ft_y_load", "misc", "ft_xyx_vloc"};
 
 void set_error(const char* fmt, ...) {
   char buf[512];
@@ -600,7 +600,7 @@ qbg_status qbg_plan_create(const qbg_basis_desc* bd, int np0, int np1, int np2,
     qbg_plan_destroy(p);
     return st;
   }
-  p->chunk = (precision == QBG_PREC_MIXED || precision == QBG_PREC_MIXED_NL64) ? 16 : 8;
+  p->chunk = 32;  // states per transform launch group
   *out = p;
   return QBG_OK;
 }

@@ -44,7 +44,10 @@ namespace qbg {
 constexpr int TC_M = 128;          // rows per tile (A)
 constexpr int TC_N = 128;          // rows per tile (B) = MMA N
 constexpr int TC_KS = 32;          // K elements per pipeline stage
-constexpr int TC_STAGES = 4;
+#ifndef QBG_TC_STAGES
+#define QBG_TC_STAGES 4
+#endif
+constexpr int TC_STAGES = QBG_TC_STAGES;
 constexpr int TC_CHUNK = 8;        // stages per tensor-memory chunk (K = 256)
 constexpr int TC_BLOCK_BYTES = TC_M * TC_KS * 2;   // 8 KB per piece per stage
 constexpr int TC_STAGE_BYTES = 4 * TC_BLOCK_BYTES; // A0 A1 B0 B1
@@ -181,23 +184,27 @@ __global__ void k_rowmax_c64(const double2* __restrict__ x, int ld, int ncols,
   if (threadIdx.x == 0) rmax[n] = red[0];
 }
 
-// pieces of the interleaved real view of x[n][g] (K = 2*ncols), scaled per row
-__global__ void k_split_rows(const double2* __restrict__ x, int ld, int ncols,
-                             const double* __restrict__ rmax, __half* __restrict__ Y,
-                             int nRT, int nKS, float* __restrict__ rscale) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+// pieces of the interleaved real view of x[n][g] (K = 2*ncols), scaled per
+// row; 4 complex elements (8 consecutive K, one 16-byte run of the canonical
+// layout per piece) per thread, so every store fills whole sectors
+__global__ void k_split_rows4(const double2* __restrict__ x, int ld, int ncols,
+                              const double* __restrict__ rmax, __half* __restrict__ Y,
+                              int nRT, int nKS, float* __restrict__ rscale) {
+  const int g0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
   const int n = blockIdx.y;
   const int e = scale_exp(rmax[n]);
-  if (g == 0) rscale[n] = ldexpf(1.f, e);
-  if (g >= ncols) return;
-  const double2 a = x[(size_t)n * ld + g];
-  __half hi, lo;
-  split2d(ldexp(a.x, -e), hi, lo);
-  Y[tc_index(0, n, 2 * g, nRT, nKS)] = hi;
-  Y[tc_index(1, n, 2 * g, nRT, nKS)] = lo;
-  split2d(ldexp(a.y, -e), hi, lo);
-  Y[tc_index(0, n, 2 * g + 1, nRT, nKS)] = hi;
-  Y[tc_index(1, n, 2 * g + 1, nRT, nKS)] = lo;
+  if (g0 == 0) rscale[n] = ldexpf(1.f, e);
+  if (g0 >= ncols) return;
+  __align__(16) __half hi[8], lo[8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int g = g0 + j;
+    const double2 a = g < ncols ? x[(size_t)n * ld + g] : make_double2(0.0, 0.0);
+    split2d(ldexp(a.x, -e), hi[2 * j], lo[2 * j]);
+    split2d(ldexp(a.y, -e), hi[2 * j + 1], lo[2 * j + 1]);
+  }
+  *reinterpret_cast<uint4*>(Y + tc_index(0, n, 2 * g0, nRT, nKS)) = *reinterpret_cast<uint4*>(hi);
+  *reinterpret_cast<uint4*>(Y + tc_index(1, n, 2 * g0, nRT, nKS)) = *reinterpret_cast<uint4*>(lo);
 }
 
 // ------------------------------------------------------------ PTX helpers
@@ -645,8 +652,8 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
     PhaseTimer pt(p, PH_MISC, st);
     k_rowmax_c64<<<nst, 256, 0, st>>>(psi, ld, ngw, t->rmax);
     QBG_LAUNCHED(p);
-    k_split_rows<<<dim3((ngw + 255) / 256, nst), 256, 0, st>>>(psi, ld, ngw, t->rmax, t->Y, nRT,
-                                                              t->x1_KS, t->sY);
+    k_split_rows4<<<dim3((ngw + 1023) / 1024, nst), 256, 0, st>>>(psi, ld, ngw, t->rmax, t->Y,
+                                                                 nRT, t->x1_KS, t->sY);
     QBG_LAUNCHED(p);
   }
   // GEMM1 with split K
@@ -684,8 +691,8 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
     QBG_LAUNCHED(p);
     k_rowmax_c64<<<nst, 256, 0, st>>>(t->fnl, P, P, t->rmax);
     QBG_LAUNCHED(p);
-    k_split_rows<<<dim3((P + 255) / 256, nst), 256, 0, st>>>(t->fnl, P, P, t->rmax, t->F, nRT,
-                                                            t->x2_KS, t->sF);
+    k_split_rows4<<<dim3((P + 1023) / 1024, nst), 256, 0, st>>>(t->fnl, P, P, t->rmax, t->F,
+                                                               nRT, t->x2_KS, t->sF);
     QBG_LAUNCHED(p);
   }
   // GEMM2 writes the NL part of H psi
