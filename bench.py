@@ -225,51 +225,72 @@ def time_etrs(H, p, occ, dt, A, steps, warmup, stream):
 
 
 # ------------------------------------------------------------ roofline
-def phase_model(H, cell, basis, nst):
-    """Per-launch algorithmic work of each phase: (kind, amount) where kind is
-    'flop' (5 n log2 n per 1-D transform, the reference's own FFT model in
-    testFourierTransform.cc; 2*M*N*K per real GEMM product on the tensor
-    pipe) or 'byte' (compulsory HBM bytes)."""
+# FP32-pipe instructions of one double-float line transform, counted by
+# instantiating the codelets of qbg_fft_engine.cuh with an operation-counting
+# scalar (double-float add 8 instructions, multiply 4, halving 2): 120 = 8 x 15
+# prime-factor = 15 dft8 (432) + 8 dft15 (1500); 48 = 3 dft16 (1280) + 16 dft3
+# (108).  Other lengths: the 120 ratio to the 5 n log2 n model.
+DF32_INST_PER_LINE = {120: 18480.0, 48: 5568.0}
+
+
+def _fft_flops(n):
+    return 5.0 * n * np.log2(n)
+
+
+def _df32_inst(n):
+    return DF32_INST_PER_LINE.get(n, _fft_flops(n) * 18480.0 / _fft_flops(120))
+
+
+def phase_model(H, cell, basis):
+    """Algorithmic work per STATE of each timed phase: (amount, bound, peak).
+
+    Transform phases count line transforms: for double-float forms the amount
+    is 2 x the FP32-pipe instructions of the algorithm (FFMA-equivalent
+    flops, against the FP32 FFMA peak); for FP64 and FP32 forms the 5 n log2 n
+    flops of the reference's own FFT model (src/tests/testFourierTransform.cc)
+    against the FP64 or FP32 peak.  GEMM phases count 2 M N K per real
+    product (3 split products on the tensor pipe in the mixed forms)."""
     n0, n1, n2 = cell.grid
     ngw, nrods = basis.ngw, basis.nrods
     nband = 2 * (max(abs(basis.idxmin[1]), abs(basis.idxmax[1])) + 1)
     P = nproj_of(cell)
-    ch = H.chunk
-    f = lambda n: 5.0 * n * np.log2(n)
-    fft64 = H.precision in ("fp64", "mixed_fft64")
-    tc = H.precision in ("mixed", "mixed_fft64")
-    m = {}
-    m["ft_z_bwd"] = ("flop", ch * nrods * f(n2))
-    m["ft_x_bwd"] = ("flop", ch * n2 * nband * f(n0))
-    m["ft_y_vloc"] = ("flop", ch * n2 * n0 * 2 * f(n1))
-    m["ft_x_fwd"] = m["ft_x_bwd"]
-    m["ft_z_fwd"] = m["ft_z_bwd"]
-    gemm = 8.0 * P * ngw * nst          # one complex GEMM
-    m["fnl_gemm"] = ("flop", 3 * gemm if tc else gemm)   # 3 split products on the tensor pipe
-    m["enl_hpsi"] = ("flop", 3 * gemm if tc else gemm)
-    bounds = {}
-    for k in m:
-        if k.startswith("ft_"):
-            bounds[k] = ("fp64", 1.007) if fft64 else ("fp32", 72.2)
-        else:
-            bounds[k] = ("tensor", None) if tc else ("fp64", 1.007)
-    return m, bounds
+    prec = H.precision
+    if prec == "mixed_df32":
+        w, fb = (lambda n: 2.0 * _df32_inst(n)), ("fp32", 72.2)
+    elif prec in ("fp64", "mixed_fft64"):
+        w, fb = _fft_flops, ("fp64", 1.007)
+    else:
+        w, fb = _fft_flops, ("fp32", 72.2)
+    tc = prec in ("mixed", "mixed_fft64", "mixed_df32")
+    lines = {
+        "ft_z_bwd": nrods * w(n2),
+        "ft_z_fwd": nrods * w(n2),
+        "ft_x_bwd": n2 * nband * w(n0),
+        "ft_x_fwd": n2 * nband * w(n0),
+        "ft_y_vloc": n2 * n0 * 2 * w(n1),
+        "ft_xyx_vloc": n2 * (2 * nband * w(n0) + 2 * n0 * w(n1)),
+        "ft_y_density": n2 * (nband * w(n0) + n0 * w(n1)),
+    }
+    m = {k: (v, fb) for k, v in lines.items()}
+    gemm = 8.0 * P * ngw  # one complex GEMM, per state
+    m["fnl_gemm"] = (3 * gemm if tc else gemm, ("tensor", None) if tc else ("fp64", 1.007))
+    m["enl_hpsi"] = m["fnl_gemm"]
+    return m
 
 
 def nproj_of(cell):
     return cell.natoms * (cell.lmax + 1) ** 2
 
 
-def roofline_of(H, cell, basis, prof, peaks):
-    model, bounds = phase_model(H, cell, basis, cell.nst)
-    dom = max(model, key=lambda k: prof.get(k, (0, 0))[0])
+def roofline_of(H, cell, basis, prof, peaks, nst):
+    """The dominant phase of one H application (largest device time)."""
+    model = phase_model(H, cell, basis)
+    dom = max((k for k in model if k in prof and prof[k][1]), key=lambda k: prof[k][0])
     tot_ms, nl = prof[dom]
-    per_launch_s = tot_ms / 1000.0 / max(nl, 1)
-    kind, amount = model[dom]
-    bound, peak = bounds[dom]
+    amount, (bound, peak) = model[dom]
     if bound == "tensor":
         peak = float(peaks.get("bf16_tflops", 1917.4))
-    achieved = amount / per_launch_s / 1e12
+    achieved = amount * nst / (tot_ms / 1000.0) / 1e12
     traffic = None
     try:
         tr = json.load(open(os.path.join(HERE, "profiles", "traffic.json")))
@@ -278,12 +299,19 @@ def roofline_of(H, cell, basis, prof, peaks):
             traffic = tr[key]["bytes_per_launch"]
     except (OSError, ValueError):
         pass
+    unit = ("TFLOP/s (FFMA-equivalent: 2 x FP32-pipe instructions of the double-float "
+            "algorithm per second)" if H.precision == "mixed_df32" and dom.startswith("ft_")
+            else "TFLOP/s")
     return {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
-            "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-            "per_launch_ms": per_launch_s * 1e3,
+            "unit": unit, "frac": achieved / peak, "traffic": traffic,
+            "per_launch_ms": tot_ms / max(nl, 1), "launches_per_H": nl,
             "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 kind::f16 runs at the same "
                             "rate)" if bound == "tensor" else "profiles/peaks_gb300.txt"),
-            "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]}}
+            "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
+            "phase_frac_of_peak": {k: round(model[k][0] * nst / (v[0] / 1000.0) / 1e12 /
+                                            (float(peaks.get("bf16_tflops", 1917.4))
+                                             if model[k][1][0] == "tensor" else model[k][1][1]), 4)
+                                   for k, v in prof.items() if v[1] and k in model}}
 
 
 # ------------------------------------------------------------ CPU baseline
@@ -407,7 +435,7 @@ def run_ours(args, rank, world, local):
     prof_rho = {k: round(v[0], 3) for k, v in H.profile_read().items() if v[1]}
     H.profile(False)
     del rho_t
-    roofline = roofline_of(H, cell, basis, prof, peaks)
+    roofline = roofline_of(H, cell, basis, prof, peaks, cell.nst)
     roofline["phases_ms_per_density"] = prof_rho
 
     # end to end through the public API with host buffers

@@ -348,12 +348,15 @@ k_sum_slots(const ST* __restrict__ slots, int nslots, long long n, double* __res
 // three-kernel path never leaves the SM.  Needs prime-factor lengths along
 // x and y that run in place, and the band rows plus one column group within
 // one CTA's shared memory.
-constexpr int kXyxThreads = 512;
+#ifndef QBG_XYX_THREADS
+#define QBG_XYX_THREADS 512
+#endif
+constexpr int kXyxThreads = QBG_XYX_THREADS;
 
 template <typename T, int X1, int X2, int Y1, int Y2>
 __global__ void __launch_bounds__(kXyxThreads, 1)
-k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const RodInfo* __restrict__ rods, int nband,
-           int n2, const int* __restrict__ band_y, const T* __restrict__ v, int G) {
+k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
+           const int* __restrict__ row_xb, int nband, int n2, const T* __restrict__ v, int G) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   constexpr int n0 = X1 * X2, n1 = Y1 * Y2, ls0 = n0 + 1, ls1 = n1 + 1;
@@ -365,9 +368,10 @@ k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const RodInfo* __restrict__ rods,
   const size_t plane = (size_t)n0 * n1;
   for (int i = threadIdx.x; i < nband * ls0; i += blockDim.x) Xb[i] = czero<T>();
   __syncthreads();
-  for (int r = threadIdx.x; r < nrods; r += blockDim.x) {
-    const int xb = rods[r].xb;
-    Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[r];
+  // band-row order: consecutive threads fill consecutive x of one row
+  for (int q = threadIdx.x; q < nrods; q += blockDim.x) {
+    const int xb = row_xb[q];
+    Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[row_rod[q]];
   }
   __syncthreads();
   constexpr int rg = kXyxThreads / X1;  // rows per in-place group
@@ -453,9 +457,9 @@ k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const RodInfo* __restrict__ rods,
   }
   for (int b0 = 0; b0 < nband; b0 += rg)
     pfa_lines<X1, X2, -1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
-  for (int r = threadIdx.x; r < nrods; r += blockDim.x) {
-    const int xb = rods[r].xb;
-    Zr[r] = Xb[(xb >> 16) * ls0 + (xb & 0xffff)];
+  for (int q = threadIdx.x; q < nrods; q += blockDim.x) {
+    const int xb = row_xb[q];
+    Zr[row_rod[q]] = Xb[(xb >> 16) * ls0 + (xb & 0xffff)];
   }
 }
 
@@ -470,8 +474,8 @@ template <> struct SlotOf<df32> { using type = df32; };
 
 template <typename T, int X1, int X2, int Y1, int Y2>
 __global__ void __launch_bounds__(kXyxThreads, 1)
-k_xy_density(const cplx<T>* __restrict__ Z, int nrods, const RodInfo* __restrict__ rods,
-             int nband, int n2, const double* __restrict__ w,
+k_xy_density(const cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
+             const int* __restrict__ row_xb, int nband, int n2, const double* __restrict__ w,
              typename SlotOf<T>::type* __restrict__ slots, int accumulate, int G) {
   using C = cplx<T>;
   using M = PfaMap<Y1, Y2>;
@@ -487,9 +491,10 @@ k_xy_density(const cplx<T>* __restrict__ Z, int nrods, const RodInfo* __restrict
   const T ws = T(w[s]);
   for (int i = threadIdx.x; i < nband * ls0; i += blockDim.x) Xb[i] = czero<T>();
   __syncthreads();
-  for (int r = threadIdx.x; r < nrods; r += blockDim.x) {
-    const int xb = rods[r].xb;
-    Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[r];
+  // band-row order: consecutive threads fill consecutive x of one row
+  for (int q = threadIdx.x; q < nrods; q += blockDim.x) {
+    const int xb = row_xb[q];
+    Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[row_rod[q]];
   }
   __syncthreads();
   constexpr int rg = kXyxThreads / X1;
@@ -826,7 +831,7 @@ static qbg_status run_xyx_(qbg_plan* p, int ns, int G, size_t sm, cudaStream_t s
   const T* v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vrdf;
   PhaseTimer pt(p, PH_XYX_VLOC, st);
   k_xyx_vloc<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), kXyxThreads, sm, st>>>(
-      (cplx<T>*)p->d_Z, p->nrods, p->d_rods, p->nband, p->np2, p->d_band_y, v, G);
+      (cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, v, G);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
@@ -840,7 +845,7 @@ static qbg_status run_xy_density_(qbg_plan* p, int ns, const double* w, int acc,
   QBG_CUDA(prep(k_xy_density<T, X1, X2, Y1, Y2>, sm));
   PhaseTimer pt(p, PH_Y_DENSITY, st);
   k_xy_density<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), kXyxThreads, sm, st>>>(
-      (const cplx<T>*)p->d_Z, p->nrods, p->d_rods, p->nband, p->np2, w,
+      (const cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, w,
       (typename SlotOf<T>::type*)p->d_rho_slots, acc, G);
   QBG_LAUNCHED(p);
   return QBG_OK;

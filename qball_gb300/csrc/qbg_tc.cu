@@ -165,13 +165,16 @@ __global__ void k_split_x2(const double2* __restrict__ anl, int nproj, int ngw,
   }
 }
 
-// per-row max |x| of a complex FP64 block [nrows][ld] (first ncols complex)
+// row maxima of |re|, |im| of x[n][0..ncols): blocks (chunk, row), the block
+// maxima combined with an integer atomicMax on the bit patterns (for
+// non-negative doubles the order of the bits is the order of the values);
+// rmax must be zero on entry
 __global__ void k_rowmax_c64(const double2* __restrict__ x, int ld, int ncols,
                              double* __restrict__ rmax) {
   __shared__ double red[256];
-  const int n = blockIdx.x;
+  const int n = blockIdx.y;
   double m = 0.0;
-  for (int g = threadIdx.x; g < ncols; g += blockDim.x) {
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ncols; g += gridDim.x * blockDim.x) {
     const double2 a = x[(size_t)n * ld + g];
     m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
   }
@@ -181,7 +184,9 @@ __global__ void k_rowmax_c64(const double2* __restrict__ x, int ld, int ncols,
     if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) rmax[n] = red[0];
+  if (threadIdx.x == 0)
+    atomicMax(reinterpret_cast<unsigned long long*>(rmax) + n,
+              (unsigned long long)__double_as_longlong(red[0]));
 }
 
 // pieces of the interleaved real view of x[n][g] (K = 2*ncols), scaled per
@@ -195,13 +200,23 @@ __global__ void k_split_rows4(const double2* __restrict__ x, int ld, int ncols,
   const int e = scale_exp(rmax[n]);
   if (g0 == 0) rscale[n] = ldexpf(1.f, e);
   if (g0 >= ncols) return;
+  // the split works on x 2^-e rounded to FP32 (24 bits, more than the 22 the
+  // two pieces keep): one FP64-pipe conversion per value instead of the
+  // FP64 scaling and residual, as GB300 runs FP64 at 1/72 of FP32.  For
+  // |e| <= 100 the power of two is applied after the conversion (values
+  // that underflow FP32 are below 2^-110 of the row maximum).
+  const bool fscale = e > -100 && e < 100;
+  const float sf = fscale ? ldexpf(1.f, -e) : 1.f;
+  const double sd = ldexp(1.0, -e);
   __align__(16) __half hi[8], lo[8];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int g = g0 + j;
     const double2 a = g < ncols ? x[(size_t)n * ld + g] : make_double2(0.0, 0.0);
-    split2d(ldexp(a.x, -e), hi[2 * j], lo[2 * j]);
-    split2d(ldexp(a.y, -e), hi[2 * j + 1], lo[2 * j + 1]);
+    const float xr = fscale ? __double2float_rn(a.x) * sf : __double2float_rn(a.x * sd);
+    const float xi = fscale ? __double2float_rn(a.y) * sf : __double2float_rn(a.y * sd);
+    split2(xr, hi[2 * j], lo[2 * j]);
+    split2(xi, hi[2 * j + 1], lo[2 * j + 1]);
   }
   *reinterpret_cast<uint4*>(Y + tc_index(0, n, 2 * g0, nRT, nKS)) = *reinterpret_cast<uint4*>(hi);
   *reinterpret_cast<uint4*>(Y + tc_index(1, n, 2 * g0, nRT, nKS)) = *reinterpret_cast<uint4*>(lo);
@@ -650,7 +665,9 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
   }
   {
     PhaseTimer pt(p, PH_MISC, st);
-    k_rowmax_c64<<<nst, 256, 0, st>>>(psi, ld, ngw, t->rmax);
+    QBG_CUDA(cudaMemsetAsync(t->rmax, 0, sizeof(double) * nst, st));
+    k_rowmax_c64<<<dim3(std::min(32, (ngw + 255) / 256), nst), 256, 0, st>>>(psi, ld, ngw,
+                                                                           t->rmax);
     QBG_LAUNCHED(p);
     k_split_rows4<<<dim3((ngw + 1023) / 1024, nst), 256, 0, st>>>(psi, ld, ngw, t->rmax, t->Y,
                                                                  nRT, t->x1_KS, t->sY);
@@ -689,7 +706,9 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
     k_tc_fnl_reduce<<<rb, 256, 0, st>>>(t->part, nsplit, 2 * P, nst, p->d_pwt, d_occ, t->fnl,
                                         enl_part);
     QBG_LAUNCHED(p);
-    k_rowmax_c64<<<nst, 256, 0, st>>>(t->fnl, P, P, t->rmax);
+    QBG_CUDA(cudaMemsetAsync(t->rmax, 0, sizeof(double) * nst, st));
+    k_rowmax_c64<<<dim3(std::min(32, (P + 255) / 256), nst), 256, 0, st>>>(t->fnl, P, P,
+                                                                         t->rmax);
     QBG_LAUNCHED(p);
     k_split_rows4<<<dim3((P + 1023) / 1024, nst), 256, 0, st>>>(t->fnl, P, P, t->rmax, t->F,
                                                                nRT, t->x2_KS, t->sF);
