@@ -64,4 +64,52 @@ struct __align__(16) df32c {
   df32 x, y;
 };
 
+// FP64 -> double-float from the bit pattern, with no FP64 instruction (GB300
+// runs FP64 at 1/72 of the FP32 rate, conversions included): hi takes the
+// 24 leading significand bits (truncated), lo the next 23 as an exact
+// integer times a power of two, so hi + lo carries 47 bits of x.  |x| below
+// 2^-80 (lo) or 2^-126 (hi) flushes to zero: the path's values are
+// normalised to order one.
+__device__ __forceinline__ df32 df32_from_f64(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+  const int E = (int)((b >> 52) & 0x7FF);
+  const int fe = E - 1023 + 127;
+  if (fe <= 0) return df32(0.f, 0.f);
+  const float hi = __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((b >> 29) & 0x7FFFFF));
+  const int le = E - 1069 + 127;  // exponent of the lo part's unit
+  float lo = 0.f;
+  if (le > 0) {
+    const unsigned r = (unsigned)(b & 0x1FFFFFFFu) >> 6;  // 23 bits
+    const float mag = __uint_as_float(0x4B000000u | r) - 8388608.0f;  // exact integer r
+    lo = __uint_as_float(sign | __float_as_uint(mag * __uint_as_float((unsigned)le << 23)));
+  }
+  return df32(hi, lo);
+}
+// FP64 -> FP32 by truncating the significand to 24 bits (relative error
+// below 2^-23), from the bit pattern: no FP64 instruction.  |x| below 2^-126
+// gives zero.
+__device__ __forceinline__ float f32_trunc_from_f64(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int fe = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+  if (fe <= 0) return 0.f;
+  return __uint_as_float(((unsigned)(b >> 32) & 0x80000000u) | ((unsigned)fe << 23) |
+                         (unsigned)((b >> 29) & 0x7FFFFF));
+}
+// FP32 -> FP64 from the bit pattern (exact for normal numbers; zero and
+// subnormal inputs give zero), no FP64 instruction
+__device__ __forceinline__ double f64_from_f32(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xFF;
+  if (e == 0) return 0.0;
+  const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                               ((unsigned long long)(e - 127 + 1023) << 52) |
+                               ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)b);
+}
+// double-float -> FP64: one FP64 add
+__device__ __forceinline__ double f64_from_df32(df32 a) {
+  return f64_from_f32(a.hi) + f64_from_f32(a.lo);
+}
+
 }  // namespace qbg

@@ -45,6 +45,9 @@ __device__ __forceinline__ void cp_async(void* dst, const void* src) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+template <typename T> __device__ __forceinline__ T from_f64(double x) { return (T)x; }
+template <> __device__ __forceinline__ df32 from_f64<df32>(double x) { return df32_from_f64(x); }
+
 template <typename T> __device__ __forceinline__ cplx<T> czero() {
   cplx<T> c;
   c.x = T(0);
@@ -78,8 +81,8 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
       if (z < 0) z += n2;
       const double2 v = ps[ri.first + i];
       C c;
-      c.x = (T)v.x;
-      c.y = (T)v.y;
+      c.x = from_f64<T>(v.x);
+      c.y = from_f64<T>(v.y);
       A[rl * ls + z] = c;
     }
   }
@@ -131,8 +134,33 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
       C vt = R[rl * ls + z];
       vt.x *= scale;
       vt.y *= scale;
-      const double2 v = make_double2((double)vt.x, (double)vt.y);
       const int g = ri.first + i;
+      if constexpr (std::is_same<T, df32>::value && MODE == 1) {
+        // double-float arithmetic; FP64 only for the two adds of each
+        // stored component (out, and acc in FP64)
+        const double2 c64 = psi[(size_t)s * ldp + g];
+        const df32 xk = df_scale2(df32_from_f64(kpg2[g]), 0.5f);
+        df32 ox = xk * df32_from_f64(c64.x), oy = xk * df32_from_f64(c64.y);
+        if (out_init) {
+          const double2 o0 = os[g];
+          ox = ox + df32_from_f64(o0.x);
+          oy = oy + df32_from_f64(o0.y);
+        }
+        ox = ox + vt.x;
+        oy = oy + vt.y;
+        os[g] = make_double2(f64_from_df32(ox), f64_from_df32(oy));
+        if (acc) {
+          double2* a = acc + (size_t)s * lda + g;
+          const df32 fx = df32_from_f64(fac.x), fy = df32_from_f64(fac.y);
+          const df32 ix = fx * ox - fy * oy, iy = fx * oy + fy * ox;
+          double2 t = *a;
+          t.x = t.x + f64_from_df32(ix);
+          t.y = t.y + f64_from_df32(iy);
+          *a = t;
+        }
+        continue;
+      }
+      const double2 v = make_double2((double)vt.x, (double)vt.y);
       if (MODE == 0) {
         os[g] = v;
       } else {

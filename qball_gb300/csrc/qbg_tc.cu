@@ -171,22 +171,25 @@ __global__ void k_split_x2(const double2* __restrict__ anl, int nproj, int ngw,
 // rmax must be zero on entry
 __global__ void k_rowmax_c64(const double2* __restrict__ x, int ld, int ncols,
                              double* __restrict__ rmax) {
-  __shared__ double red[256];
+  // maxima of |x| compared as the integer bit patterns with the sign
+  // cleared (no FP64 instruction)
+  __shared__ unsigned long long red[256];
   const int n = blockIdx.y;
-  double m = 0.0;
+  const unsigned long long mask = 0x7FFFFFFFFFFFFFFFull;
+  unsigned long long m = 0;
   for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ncols; g += gridDim.x * blockDim.x) {
     const double2 a = x[(size_t)n * ld + g];
-    m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
+    const unsigned long long u = (unsigned long long)__double_as_longlong(a.x) & mask;
+    const unsigned long long w = (unsigned long long)__double_as_longlong(a.y) & mask;
+    m = max(m, max(u, w));
   }
   red[threadIdx.x] = m;
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    if (threadIdx.x < s) red[threadIdx.x] = max(red[threadIdx.x], red[threadIdx.x + s]);
     __syncthreads();
   }
-  if (threadIdx.x == 0)
-    atomicMax(reinterpret_cast<unsigned long long*>(rmax) + n,
-              (unsigned long long)__double_as_longlong(red[0]));
+  if (threadIdx.x == 0) atomicMax(reinterpret_cast<unsigned long long*>(rmax) + n, red[0]);
 }
 
 // pieces of the interleaved real view of x[n][g] (K = 2*ncols), scaled per
@@ -213,8 +216,8 @@ __global__ void k_split_rows4(const double2* __restrict__ x, int ld, int ncols,
   for (int j = 0; j < 4; ++j) {
     const int g = g0 + j;
     const double2 a = g < ncols ? x[(size_t)n * ld + g] : make_double2(0.0, 0.0);
-    const float xr = fscale ? __double2float_rn(a.x) * sf : __double2float_rn(a.x * sd);
-    const float xi = fscale ? __double2float_rn(a.y) * sf : __double2float_rn(a.y * sd);
+    const float xr = fscale ? f32_trunc_from_f64(a.x) * sf : __double2float_rn(a.x * sd);
+    const float xi = fscale ? f32_trunc_from_f64(a.y) * sf : __double2float_rn(a.y * sd);
     split2(xr, hi[2 * j], lo[2 * j]);
     split2(xi, hi[2 * j + 1], lo[2 * j + 1]);
   }
@@ -494,8 +497,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
             for (int j = 0; j < 32; ++j) {
               const int n = nt * TC_N + cb + j;
               if (n < args.N) {
-                const double v = ((double)__uint_as_float(h[j]) + (double)__uint_as_float(l[j])) *
-                                 (double)sa * (double)args.sB[n];
+                // sa * sB is a power of two: scaling the (hi, lo) pair in FP32 is
+                // exact, and the FP64 result then costs one FP64 add
+                const float sc = sa * args.sB[n];
+                const double v = f64_from_f32(__uint_as_float(h[j]) * sc) +
+                                 f64_from_f32(__uint_as_float(l[j]) * sc);
                 if (MODE == TC_OUT_PARTIAL)
                   args.out[((size_t)z * args.N + n) * args.M + m] = v;
                 else
