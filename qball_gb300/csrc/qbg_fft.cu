@@ -76,14 +76,26 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int rl = warp; rl < nl; rl += nw) {
     const RodInfo ri = rods[r0 + rl];
-    for (int i = lane; i < ri.size; i += 32) {
-      int z = ri.lmin + i;
-      if (z < 0) z += n2;
-      const double2 v = ps[ri.first + i];
-      C c;
-      c.x = from_f64<T>(v.x);
-      c.y = from_f64<T>(v.y);
-      A[rl * ls + z] = c;
+    // up to four coefficients per lane loaded before any is stored
+    for (int ib = 0; ib < ri.size; ib += 128) {
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = ib + lane + 32 * u;
+        if (i < ri.size) v[u] = ps[ri.first + i];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int i = ib + lane + 32 * u;
+        if (i < ri.size) {
+          int z = ri.lmin + i;
+          if (z < 0) z += n2;
+          C c;
+          c.x = from_f64<T>(v[u].x);
+          c.y = from_f64<T>(v[u].y);
+          A[rl * ls + z] = c;
+        }
+      }
     }
   }
   __syncthreads();
@@ -126,6 +138,56 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
   const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double2* os = out + (size_t)s * ldo;
+  if constexpr (std::is_same<T, df32>::value && MODE == 1) {
+    // double-float arithmetic; FP64 only for the add of each stored
+    // component.  A lane loads all its coefficients of a rod (up to four)
+    // before computing, so the epilogue's loads overlap.
+    constexpr int U = 4;
+    const df32 fx = df32_from_f64(fac.x), fy = df32_from_f64(fac.y);
+    for (int rl = warp; rl < nl; rl += nw) {
+      const RodInfo ri = rods[r0 + rl];
+      for (int ib = 0; ib < ri.size; ib += 32 * U) {
+        double2 c64[U], o0[U], a0[U];
+        double kp[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = ib + lane + 32 * u;
+          if (i < ri.size) {
+            const int g = ri.first + i;
+            c64[u] = psi[(size_t)s * ldp + g];
+            kp[u] = kpg2[g];
+            o0[u] = out_init ? os[g] : make_double2(0.0, 0.0);
+            if (acc) a0[u] = acc[(size_t)s * lda + g];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = ib + lane + 32 * u;
+          if (i < ri.size) {
+            const int g = ri.first + i;
+            int z = ri.lmin + i;
+            if (z < 0) z += n2;
+            C vt = R[rl * ls + z];
+            const df32 xk = df_scale2(df32_from_f64(kp[u]), 0.5f);
+            df32 ox = xk * df32_from_f64(c64[u].x), oy = xk * df32_from_f64(c64[u].y);
+            if (out_init) {
+              ox = ox + df32_from_f64(o0[u].x);
+              oy = oy + df32_from_f64(o0[u].y);
+            }
+            ox = ox + vt.x * scale;
+            oy = oy + vt.y * scale;
+            os[g] = make_double2(f64_from_df32(ox), f64_from_df32(oy));
+            if (acc) {
+              const df32 ix = fx * ox - fy * oy, iy = fx * oy + fy * ox;
+              acc[(size_t)s * lda + g] =
+                  make_double2(a0[u].x + f64_from_df32(ix), a0[u].y + f64_from_df32(iy));
+            }
+          }
+        }
+      }
+    }
+    return;
+  }
   for (int rl = warp; rl < nl; rl += nw) {
     const RodInfo ri = rods[r0 + rl];
     for (int i = lane; i < ri.size; i += 32) {
@@ -135,31 +197,6 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
       vt.x *= scale;
       vt.y *= scale;
       const int g = ri.first + i;
-      if constexpr (std::is_same<T, df32>::value && MODE == 1) {
-        // double-float arithmetic; FP64 only for the two adds of each
-        // stored component (out, and acc in FP64)
-        const double2 c64 = psi[(size_t)s * ldp + g];
-        const df32 xk = df_scale2(df32_from_f64(kpg2[g]), 0.5f);
-        df32 ox = xk * df32_from_f64(c64.x), oy = xk * df32_from_f64(c64.y);
-        if (out_init) {
-          const double2 o0 = os[g];
-          ox = ox + df32_from_f64(o0.x);
-          oy = oy + df32_from_f64(o0.y);
-        }
-        ox = ox + vt.x;
-        oy = oy + vt.y;
-        os[g] = make_double2(f64_from_df32(ox), f64_from_df32(oy));
-        if (acc) {
-          double2* a = acc + (size_t)s * lda + g;
-          const df32 fx = df32_from_f64(fac.x), fy = df32_from_f64(fac.y);
-          const df32 ix = fx * ox - fy * oy, iy = fx * oy + fy * ox;
-          double2 t = *a;
-          t.x = t.x + f64_from_df32(ix);
-          t.y = t.y + f64_from_df32(iy);
-          *a = t;
-        }
-        continue;
-      }
       const double2 v = make_double2((double)vt.x, (double)vt.y);
       if (MODE == 0) {
         os[g] = v;

@@ -681,8 +681,26 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
   }
   // GEMM1 with split K
   const int mt1 = t->x1_RT;
-  int nsplit = std::max(1, (3 * 152 + mt1 * nRT - 1) / (mt1 * nRT));
-  nsplit = std::min(nsplit, t->x1_KS);
+  // split K so that the CTAs (one per SM) fill their last wave: the time is
+  // ~ waves / nsplit, waves = ceil(tiles * nsplit / SMs); at least ~3 waves
+  int sms = 152;
+  {
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  const int tiles = mt1 * nRT;
+  int nsplit = 1;
+  double best = 1e30;
+  for (int ns = 1; ns <= 64 && ns <= t->x1_KS; ++ns) {
+    const int waves = (tiles * ns + sms - 1) / sms;
+    if (ns > 1 && waves > 8) break;
+    const double cost = (double)waves / ns + 0.002 * ns;  // small cost per extra partial
+    if (cost < best) {
+      best = cost;
+      nsplit = ns;
+    }
+  }
   const int ksp = (t->x1_KS + nsplit - 1) / nsplit;
   nsplit = (t->x1_KS + ksp - 1) / ksp;
   QBG_TRY_TC(ensure((void**)&t->part, &t->part_bytes, sizeof(double) * nsplit * nst * 2 * P));
