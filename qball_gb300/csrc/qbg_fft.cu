@@ -413,13 +413,18 @@ k_sum_slots(const ST* __restrict__ slots, int nslots, long long n, double* __res
 // three-kernel path never leaves the SM.  Needs prime-factor lengths along
 // x and y that run in place, and the band rows plus one column group within
 // one CTA's shared memory.
+// threads per CTA of the fused kernels: 768 for the three-pass 120-point
+// transforms (their codelets fit 80 registers), 512 for the two-pass ones
 #ifndef QBG_XYX_THREADS
 #define QBG_XYX_THREADS 512
 #endif
-constexpr int kXyxThreads = QBG_XYX_THREADS;
+#ifndef QBG_XYX_THREADS_120
+#define QBG_XYX_THREADS_120 768
+#endif
+template <int N> constexpr int xyx_threads() { return N == 120 ? QBG_XYX_THREADS_120 : QBG_XYX_THREADS; }
 
 template <typename T, int X1, int X2, int Y1, int Y2>
-__global__ void __launch_bounds__(kXyxThreads, 1)
+__global__ void __launch_bounds__(xyx_threads<X1 * X2>(), 1)
 k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
            const int* __restrict__ row_xb, int nband, int n2, const T* __restrict__ v, int G) {
   using C = cplx<T>;
@@ -439,9 +444,17 @@ k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
     Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[row_rod[q]];
   }
   __syncthreads();
-  constexpr int rg = kXyxThreads / X1;  // rows per in-place group
-  for (int b0 = 0; b0 < nband; b0 += rg)
-    pfa_lines<X1, X2, +1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  constexpr bool kP3 = X1 * X2 == 120 && Y1 * Y2 == 120;  // three-pass 8 x 3 x 5
+  constexpr int kThr = xyx_threads<X1 * X2>();
+  constexpr int rg = kThr / X1;   // rows per in-place group (two passes)
+  constexpr int rg3 = kThr / 15;  // rows per in-place group (three passes)
+  if constexpr (kP3) {
+    for (int b0 = 0; b0 < nband; b0 += rg3)
+      pfa120_lines<+1>(Xb + b0 * ls0, ls0, min(rg3, nband - b0));
+  } else {
+    for (int b0 = 0; b0 < nband; b0 += rg)
+      pfa_lines<X1, X2, +1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  }
   // y by column groups: fill, backward pass 1, backward pass 2 with the v
   // product fused into its stores, forward pass 1, forward pass 2 storing
   // only the band rows, straight into Xb
@@ -450,17 +463,55 @@ k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
   const T* vz = v + (size_t)z * plane;
   for (int c0 = 0; c0 < n0; c0 += G) {
     const int gl = min(G, n0 - c0);
+    const float igl = 1.f / (float)gl;
     for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
-      const int cl = it % gl, y = it / gl;
+      const int y = divf(it, igl), cl = it - y * gl;
       cp_async<sizeof(T)>(V + y * G + cl, vz + (size_t)y * n0 + c0 + cl);
     }
     cp_async_commit();
     for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
-      const int cl = it % gl, y = it / gl;
+      const int y = divf(it, igl), cl = it - y * gl;
       const int b = y < nlow ? y : (y >= n1 - (nband - nlow) ? y - n1 + nband : -1);
       W[cl * ls1 + y] = b >= 0 ? Xb[b * ls0 + c0 + cl] : czero<T>();
     }
     __syncthreads();
+    if constexpr (kP3) {
+      // 3- and 5-point passes, then the 8-point pass: backward with the v
+      // product in its stores, forward storing only the band rows into Xb
+      pfa120_ab<+1>(W, ls1, gl);
+      const bool act3 = (int)threadIdx.x < gl * 15;
+      const int j = divf(threadIdx.x, igl), cl3 = threadIdx.x - j * gl;
+      const int ka = divf(j, 0.2f), kb = j - 5 * ka;
+      C* ln3 = W + cl3 * ls1;
+      C w8[8];
+      if (act3) pfa120_c<+1>(ln3, ka, kb, w8);
+      cp_async_wait_all();
+      __syncthreads();
+      if (act3) {
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) {
+          const int y = pfa120_out(k1, ka, kb);
+          const T vv = V[y * G + cl3];
+          C c = w8[k1];
+          c.x = c.x * vv;
+          c.y = c.y * vv;
+          ln3[y] = c;
+        }
+      }
+      __syncthreads();
+      pfa120_ab<-1>(W, ls1, gl);
+      if (act3) {
+        pfa120_c<-1>(ln3, ka, kb, w8);
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) {
+          const int y = pfa120_out(k1, ka, kb);
+          const int bb = y < nlow ? y : (y >= n1 - (nband - nlow) ? y - n1 + nband : -1);
+          if (bb >= 0) Xb[bb * ls0 + c0 + cl3] = w8[k1];
+        }
+      }
+      __syncthreads();
+      continue;
+    }
     for (int it = threadIdx.x; it < gl * Y2; it += blockDim.x) {
       const int n2i = it / gl;
       pfa_item1<Y1, Y2, +1>(W + (it - n2i * gl) * ls1, n2i);
@@ -520,8 +571,13 @@ k_xyx_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
     }
     __syncthreads();
   }
-  for (int b0 = 0; b0 < nband; b0 += rg)
-    pfa_lines<X1, X2, -1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  if constexpr (kP3) {
+    for (int b0 = 0; b0 < nband; b0 += rg3)
+      pfa120_lines<-1>(Xb + b0 * ls0, ls0, min(rg3, nband - b0));
+  } else {
+    for (int b0 = 0; b0 < nband; b0 += rg)
+      pfa_lines<X1, X2, -1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  }
   for (int q = threadIdx.x; q < nrods; q += blockDim.x) {
     const int xb = row_xb[q];
     Zr[row_rod[q]] = Xb[(xb >> 16) * ls0 + (xb & 0xffff)];
@@ -538,7 +594,7 @@ template <typename T> struct SlotOf { using type = double; };
 template <> struct SlotOf<df32> { using type = df32; };
 
 template <typename T, int X1, int X2, int Y1, int Y2>
-__global__ void __launch_bounds__(kXyxThreads, 1)
+__global__ void __launch_bounds__(xyx_threads<X1 * X2>(), 1)
 k_xy_density(const cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
              const int* __restrict__ row_xb, int nband, int n2, const double* __restrict__ w,
              typename SlotOf<T>::type* __restrict__ slots, int accumulate, int G) {
@@ -562,28 +618,60 @@ k_xy_density(const cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ r
     Xb[(xb >> 16) * ls0 + (xb & 0xffff)] = Zr[row_rod[q]];
   }
   __syncthreads();
-  constexpr int rg = kXyxThreads / X1;
-  for (int b0 = 0; b0 < nband; b0 += rg)
-    pfa_lines<X1, X2, +1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  constexpr bool kP3 = X1 * X2 == 120 && Y1 * Y2 == 120;
+  constexpr int kThr = xyx_threads<X1 * X2>();
+  constexpr int rg = kThr / X1;
+  constexpr int rg3 = kThr / 15;
+  if constexpr (kP3) {
+    for (int b0 = 0; b0 < nband; b0 += rg3)
+      pfa120_lines<+1>(Xb + b0 * ls0, ls0, min(rg3, nband - b0));
+  } else {
+    for (int b0 = 0; b0 < nband; b0 += rg)
+      pfa_lines<X1, X2, +1, T>(Xb + b0 * ls0, nullptr, min(rg, nband - b0), ls0);
+  }
   // column groups; when accumulating, the slot tile of the group is fetched
   // with cp.async into S while the group is filled and transformed
   ST* S = reinterpret_cast<ST*>(W + G * ls1);  // [n1][G]
   const int nlow = nband / 2 + (nband & 1);
   for (int c0 = 0; c0 < n0; c0 += G) {
     const int gl = min(G, n0 - c0);
+    const float igl = 1.f / (float)gl;
     if (accumulate) {
       for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
-        const int cl = it % gl, y = it / gl;
+        const int y = divf(it, igl), cl = it - y * gl;
         cp_async<sizeof(ST)>(S + y * G + cl, rz + (size_t)y * n0 + c0 + cl);
       }
       cp_async_commit();
     }
     for (int it = threadIdx.x; it < gl * n1; it += blockDim.x) {
-      const int cl = it % gl, y = it / gl;
+      const int y = divf(it, igl), cl = it - y * gl;
       const int b = y < nlow ? y : (y >= n1 - (nband - nlow) ? y - n1 + nband : -1);
       W[cl * ls1 + y] = b >= 0 ? Xb[b * ls0 + c0 + cl] : czero<T>();
     }
     __syncthreads();
+    // (the y pass keeps the two-pass split here: with no forward half, its
+    // last pass writes straight to memory and measured faster)
+    if constexpr (kP3 && false) {
+      pfa120_ab<+1>(W, ls1, gl);
+      if (accumulate) {
+        cp_async_wait_all();
+        __syncthreads();
+      }
+      if ((int)threadIdx.x < gl * 15) {
+        const int j = divf(threadIdx.x, igl), cl3 = threadIdx.x - j * gl;
+        const int ka = divf(j, 0.2f), kb = j - 5 * ka;
+        C w8[8];
+        pfa120_c<+1>(W + cl3 * ls1, ka, kb, w8);
+#pragma unroll
+        for (int k1 = 0; k1 < 8; ++k1) {
+          const int y = pfa120_out(k1, ka, kb);
+          const T a = ws * (w8[k1].x * w8[k1].x + w8[k1].y * w8[k1].y);
+          rz[(size_t)y * n0 + c0 + cl3] = accumulate ? S[y * G + cl3] + a : a;
+        }
+      }
+      __syncthreads();
+      continue;
+    }
     for (int it = threadIdx.x; it < gl * Y2; it += blockDim.x) {
       const int n2i = it / gl;
       pfa_item1<Y1, Y2, +1>(W + (it - n2i * gl) * ls1, n2i);
@@ -895,7 +983,7 @@ static qbg_status run_xyx_(qbg_plan* p, int ns, int G, size_t sm, cudaStream_t s
   QBG_CUDA(prep(k_xyx_vloc<T, X1, X2, Y1, Y2>, sm));
   const T* v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vrdf;
   PhaseTimer pt(p, PH_XYX_VLOC, st);
-  k_xyx_vloc<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), kXyxThreads, sm, st>>>(
+  k_xyx_vloc<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), xyx_threads<X1 * X2>(), sm, st>>>(
       (cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, v, G);
   QBG_LAUNCHED(p);
   return QBG_OK;
@@ -909,7 +997,7 @@ static qbg_status run_xy_density_(qbg_plan* p, int ns, const double* w, int acc,
                                   size_t sm, cudaStream_t st) {
   QBG_CUDA(prep(k_xy_density<T, X1, X2, Y1, Y2>, sm));
   PhaseTimer pt(p, PH_Y_DENSITY, st);
-  k_xy_density<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), kXyxThreads, sm, st>>>(
+  k_xy_density<T, X1, X2, Y1, Y2><<<dim3(p->np2, ns), xyx_threads<X1 * X2>(), sm, st>>>(
       (const cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, w,
       (typename SlotOf<T>::type*)p->d_rho_slots, acc, G);
   QBG_LAUNCHED(p);
@@ -943,8 +1031,9 @@ template <typename T> static int xyx_group(const qbg_plan* p, size_t* smem) {
   const size_t base = (size_t)p->nband * (p->np0 + 1) * cs;
   const size_t per_col = (size_t)(p->np1 + 1) * cs + (size_t)p->np1 * sizeof(T);
   const size_t cap = 227 * 1024;
-  if (base + per_col > cap || kXyxThreads / dx.pfa < 1) return 0;
-  const int gmax = std::min<int>({(int)((cap - base) / per_col), kXyxThreads / dy.pfa, p->np0});
+  const int thr = p->np0 == 120 ? xyx_threads<120>() : xyx_threads<0>();
+  if (base + per_col > cap || thr / dx.pfa < 1) return 0;
+  const int gmax = std::min<int>({(int)((cap - base) / per_col), thr / dy.pfa, p->np0});
   if (gmax < 8) return 0;
   const int ngroups = (p->np0 + gmax - 1) / gmax;
   const int G = (p->np0 + ngroups - 1) / ngroups;
@@ -961,7 +1050,8 @@ template <typename T> static int xy_density_group(const qbg_plan* p, size_t* sme
   const size_t per_col = (size_t)(p->np1 + 1) * cs + (size_t)p->np1 * sizeof(double);
   const size_t cap = 227 * 1024;
   if (base + per_col > cap) return 0;
-  const int gmax = std::min<int>({(int)((cap - base) / per_col), kXyxThreads / dy.pfa, p->np0});
+  const int thr = p->np0 == 120 ? xyx_threads<120>() : xyx_threads<0>();
+  const int gmax = std::min<int>({(int)((cap - base) / per_col), thr / dy.pfa, p->np0});
   if (gmax < 8) return 0;
   const int ngroups = (p->np0 + gmax - 1) / gmax;
   const int G = (p->np0 + ngroups - 1) / ngroups;

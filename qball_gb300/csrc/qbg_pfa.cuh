@@ -132,6 +132,97 @@ __device__ __forceinline__ cplx<T>* pfa_lines(cplx<T>* A, cplx<T>* B, int nlines
   return B;
 }
 
+// ---- 120 = 8 x 3 x 5 as three prime-factor passes ------------------------
+// Nesting 15 = 3 x 5 inside 120 = 8 x 15 gives the input slot of (n1, a, b),
+// n1 < 8, a < 3, b < 5, as (15 n1 + 40 a + 24 b) mod 120 and the output index
+// of (k1, ka, kb) as (105 k1 + 40 ka + 96 kb) mod 120 (k = k1 mod 8,
+// k = 10 ka + 6 kb mod 15).  The 3-point and 5-point passes run in place on
+// the slots (40 and 24 items per line); the 8-point pass (15 items per line)
+// is left to the caller, which decides where its outputs go.  Against the
+// two-pass split the longest per-item codelet drops from 1500 to 432
+// double-float instructions, so more threads share every pass.
+__host__ __device__ __forceinline__ int pfa120_slot(int n1, int a, int b) {
+  return (15 * n1 + 40 * a + 24 * b) % 120;
+}
+__host__ __device__ __forceinline__ int pfa120_out(int k1, int ka, int kb) {
+  return (105 * k1 + 40 * ka + 96 * kb) % 120;
+}
+// x mod 120 for 0 <= x < 240
+__device__ __forceinline__ int mod120(int x) { return x >= 120 ? x - 120 : x; }
+// (q, r) = divmod(it, n) with inv = 1/n in FP32 (it < 2^20, n <= 4096)
+__device__ __forceinline__ int divf(int it, float inv) { return (int)(((float)it + 0.5f) * inv); }
+
+// the 3-point and 5-point passes over nl lines (stride ls); ends with a
+// barrier.  Slot indices advance by +40 (a) and +24 (b) modulo 120.
+template <int S, typename C>
+__device__ __forceinline__ void pfa120_ab(C* L, int ls, int nl) {
+  const float inl = 1.f / (float)nl;
+  for (int it = threadIdx.x; it < nl * 40; it += blockDim.x) {
+    const int j = divf(it, inl), line = it - j * nl;  // j = 5 n1 + b
+    const int n1 = divf(j, 0.2f), b = j - 5 * n1;
+    C* ln = L + line * ls;
+    const int i0 = pfa120_slot(n1, 0, b), i1 = mod120(i0 + 40), i2 = mod120(i1 + 40);
+    C v[3] = {ln[i0], ln[i1], ln[i2]};
+    dft3<S>(v);
+    ln[i0] = v[0];
+    ln[i1] = v[1];
+    ln[i2] = v[2];
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < nl * 24; it += blockDim.x) {
+    const int j = divf(it, inl), line = it - j * nl;  // j = 3 n1 + ka
+    const int n1 = divf(j, 1.f / 3.f), ka = j - 3 * n1;
+    C* ln = L + line * ls;
+    int idx[5];
+    idx[0] = pfa120_slot(n1, ka, 0);
+#pragma unroll
+    for (int b = 1; b < 5; ++b) idx[b] = mod120(idx[b - 1] + 24);
+    C v[5];
+#pragma unroll
+    for (int b = 0; b < 5; ++b) v[b] = ln[idx[b]];
+    dft5<S>(v);
+#pragma unroll
+    for (int b = 0; b < 5; ++b) ln[idx[b]] = v[b];
+  }
+  __syncthreads();
+}
+
+// the 8-point pass of item (ka, kb) of one line: v[k1] is the output at
+// pfa120_out(k1, ka, kb) (outputs advance by +105 modulo 120)
+template <int S, typename C>
+__device__ __forceinline__ void pfa120_c(const C* ln, int ka, int kb, C* v) {
+  int i = pfa120_slot(0, ka, kb);
+#pragma unroll
+  for (int n1 = 0; n1 < 8; ++n1) {
+    v[n1] = ln[i];
+    i = mod120(i + 15);
+  }
+  dft8<S>(v);
+}
+
+// whole transform of nl <= blockDim.x / 15 lines in place (the 8-point pass
+// holds its item in registers across a barrier); ends with a barrier
+template <int S, typename C>
+__device__ __forceinline__ void pfa120_lines(C* L, int ls, int nl) {
+  pfa120_ab<S>(L, ls, nl);
+  const bool act = (int)threadIdx.x < nl * 15;
+  const int j = divf(threadIdx.x, 1.f / (float)nl), line = threadIdx.x - j * nl;  // j = 5 ka + kb
+  const int ka = divf(j, 0.2f), kb = j - 5 * ka;
+  C v[8];
+  if (act) pfa120_c<S>(L + line * ls, ka, kb, v);
+  __syncthreads();
+  if (act) {
+    C* ln = L + line * ls;
+    int o = pfa120_out(0, ka, kb);
+#pragma unroll
+    for (int k1 = 0; k1 < 8; ++k1) {
+      ln[o] = v[k1];
+      o = mod120(o + 105);
+    }
+  }
+  __syncthreads();
+}
+
 // prime-factor split used for length n (0: none; the Stockham engine runs)
 __host__ __device__ inline int pfa_split(int n) {
   switch (n) {

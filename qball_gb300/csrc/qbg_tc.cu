@@ -48,7 +48,10 @@ constexpr int TC_KS = 32;          // K elements per pipeline stage
 #define QBG_TC_STAGES 4
 #endif
 constexpr int TC_STAGES = QBG_TC_STAGES;
-constexpr int TC_CHUNK = 8;        // stages per tensor-memory chunk (K = 256)
+#ifndef QBG_TC_CHUNK
+#define QBG_TC_CHUNK 8
+#endif
+constexpr int TC_CHUNK = QBG_TC_CHUNK;  // stages per tensor-memory chunk (K = 256)
 constexpr int TC_BLOCK_BYTES = TC_M * TC_KS * 2;   // 8 KB per piece per stage
 constexpr int TC_STAGE_BYTES = 4 * TC_BLOCK_BYTES; // A0 A1 B0 B1
 constexpr int TC_THREADS = 192;
