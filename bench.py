@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--fp64-warmup", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--cpu-states", type=int, default=16)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
@@ -446,6 +447,13 @@ def run_ours(args, rank, world, local):
         h_in.copy_(psi)
         h_out = torch.empty_like(h_in, pin_memory=True)
         J = None
+        # one untimed step through the same calls (first-call set-up of the
+        # current and the copies stays out of the timed region)
+        for _ in range(args.e2e_warmup):
+            p.copy_(h_in, non_blocking=True)
+            H.etrs_step(p, occ, args.dt, A_t=A, A_tdt=A, stream=stream)
+            J = H.current(p, occ, float(occ.sum()), stream=stream)
+            h_out.copy_(p, non_blocking=True)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -462,7 +470,8 @@ def run_ours(args, rank, world, local):
         e2e_ms = allreduce_max(e0.elapsed_time(e1), world)
         e2e = {"value": world * args.e2e_steps / (e2e_ms / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes + 24,
-               "steps": args.e2e_steps, "wall_s": wall, "J_last": list(map(float, J))}
+               "steps": args.e2e_steps, "warmup": args.e2e_warmup, "wall_s": wall,
+               "J_last": list(map(float, J))}
         del h_in, h_out
     del H
     torch.cuda.empty_cache()

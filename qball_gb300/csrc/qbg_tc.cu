@@ -54,7 +54,10 @@ constexpr int TC_STAGES = QBG_TC_STAGES;
 constexpr int TC_CHUNK = QBG_TC_CHUNK;  // stages per tensor-memory chunk (K = 256)
 constexpr int TC_BLOCK_BYTES = TC_M * TC_KS * 2;   // 8 KB per piece per stage
 constexpr int TC_STAGE_BYTES = 4 * TC_BLOCK_BYTES; // A0 A1 B0 B1
-constexpr int TC_THREADS = 192;
+constexpr int TC_THREADS = 576;    // producer, MMA issuer, 16 epilogue warps
+constexpr int TC_NBUF = 4;         // tensor-memory chunk buffers (4 x 128 columns)
+constexpr int TC_EPI = 512;        // epilogue threads
+constexpr int TC_ECOLS = 32;       // columns per epilogue thread
 constexpr int TC_SPIN = 1 << 21;   // polls per bounded wait (~0.2 s with backoff)
 
 // byte offset of element (r, k) inside one 128x32 block image
@@ -334,8 +337,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
   uint64_t* full = (uint64_t*)(smem + TC_STAGES * TC_STAGE_BYTES);
   uint64_t* empty = full + TC_STAGES;
   uint64_t* accfull = empty + TC_STAGES;
-  uint64_t* accempty = accfull + 2;
-  uint64_t* drain = accempty + 2;
+  uint64_t* accempty = accfull + TC_NBUF;
+  uint64_t* drain = accempty + TC_NBUF;
   uint32_t* tmem_slot = (uint32_t*)(drain + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
@@ -353,10 +356,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    mbar_init(&accfull[0], 1);
-    mbar_init(&accfull[1], 1);
-    mbar_init(&accempty[0], 128);
-    mbar_init(&accempty[1], 128);
+    for (int b = 0; b < TC_NBUF; ++b) {
+      mbar_init(&accfull[b], 1);
+      mbar_init(&accempty[b], TC_EPI);
+    }
     mbar_init(drain, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -405,8 +408,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       const uint32_t idesc = idesc_f16_f32(TC_M, TC_N);
       int i = 0;
       for (int c = 0; c < nchunks && !*abort_flag; ++c) {
-        const int b = c & 1;
-        if (c >= 2 && !mbar_wait(&accempty[b], ((c >> 1) - 1) & 1, args.status)) {
+        const int b = c % TC_NBUF;
+        if (c >= TC_NBUF && !mbar_wait(&accempty[b], ((c / TC_NBUF) - 1) & 1, args.status)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
           break;
@@ -444,72 +447,64 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       mma_commit(drain);
       mbar_wait(drain, 0, args.status);
     } else if (warp >= 2) {
-      // ---------------- epilogue: fold each chunk into the (hi, lo) sums
-      const int q = warp & 3;  // tensor memory lane quarter of this warp
+      // ---------------- epilogue: fold each chunk into compensated (hi, lo)
+      // sums held in registers.  Warp w reads tensor-memory lane quarter
+      // w & 3 (rows) and column block (w - 2) >> 2 (32 of the 128 columns).
+      const int q = warp & 3;
+      const int cbase = ((warp - 2) >> 2) * TC_ECOLS;
       const uint32_t lane_off = (uint32_t)(q * 32) << 16;
+      float hi[TC_ECOLS], lo[TC_ECOLS];
+#pragma unroll
+      for (int j = 0; j < TC_ECOLS; ++j) {
+        hi[j] = 0.f;
+        lo[j] = 0.f;
+      }
+      bool ok = true;
       for (int c = 0; c < nchunks; ++c) {
-        const int b = c & 1;
-        if (!mbar_wait(&accfull[b], (c >> 1) & 1, args.status)) {
+        const int b = c % TC_NBUF;
+        if (!mbar_wait(&accfull[b], (c / TC_NBUF) & 1, args.status)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
+          ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        for (int cb = 0; cb < 128; cb += 32) {
-          uint32_t p[32], h[32], l[32];
-          tmem_ld32(tbase + lane_off + b * 128 + cb, p);
-          if (c > 0) {
-            tmem_ld32(tbase + lane_off + 256 + cb, h);
-            tmem_ld32(tbase + lane_off + 384 + cb, l);
-          }
+#pragma unroll
+        for (int cb = 0; cb < TC_ECOLS; cb += 32) {
+          uint32_t p[32];
+          tmem_ld32(tbase + lane_off + b * 128 + cbase + cb, p);
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const float x = __uint_as_float(p[j]);
-            if (c == 0) {
-              h[j] = p[j];
-              l[j] = 0u;
-            } else {
-              const float a = __uint_as_float(h[j]);
-              const float s = a + x;
-              const float bb = s - a;
-              const float e = (a - (s - bb)) + (x - bb);
-              h[j] = __float_as_uint(s);
-              l[j] = __float_as_uint(__uint_as_float(l[j]) + e);
-            }
+            const float a = hi[cb + j];
+            const float s = a + x;
+            const float bb = s - a;
+            const float e = (a - (s - bb)) + (x - bb);
+            hi[cb + j] = s;
+            lo[cb + j] += e;
           }
-          tmem_st32(tbase + lane_off + 256 + cb, h);
-          tmem_st32(tbase + lane_off + 384 + cb, l);
-          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         mbar_arrive(&accempty[b]);
       }
-      // final write
-      if (!*abort_flag) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // final write from the registers
+      if (ok && !*abort_flag) {
         const int m = mt * TC_M + q * 32 + lane;
-        const float sa = m < args.M ? args.sA[m] : 0.f;
-        for (int cb = 0; cb < 128; cb += 32) {
-          uint32_t h[32], l[32];
-          tmem_ld32(tbase + lane_off + 256 + cb, h);
-          tmem_ld32(tbase + lane_off + 384 + cb, l);
-          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-          if (m < args.M) {
+        if (m < args.M) {
+          const float sa = args.sA[m];
 #pragma unroll
-            for (int j = 0; j < 32; ++j) {
-              const int n = nt * TC_N + cb + j;
-              if (n < args.N) {
-                // sa * sB is a power of two: scaling the (hi, lo) pair in FP32 is
-                // exact, and the FP64 result then costs one FP64 add
-                const float sc = sa * args.sB[n];
-                const double v = f64_from_f32(__uint_as_float(h[j]) * sc) +
-                                 f64_from_f32(__uint_as_float(l[j]) * sc);
-                if (MODE == TC_OUT_PARTIAL)
-                  args.out[((size_t)z * args.N + n) * args.M + m] = v;
-                else
-                  args.out[(size_t)n * 2 * args.ldo + m] = v;
-              }
+          for (int j = 0; j < TC_ECOLS; ++j) {
+            const int n = nt * TC_N + cbase + j;
+            if (n < args.N) {
+              // sa * sB is a power of two: scaling the (hi, lo) pair in FP32
+              // is exact, and the FP64 result then costs one FP64 add
+              const float sc = sa * args.sB[n];
+              const double v = f64_from_f32(hi[j] * sc) + f64_from_f32(lo[j] * sc);
+              if (MODE == TC_OUT_PARTIAL)
+                args.out[((size_t)z * args.N + n) * args.M + m] = v;
+              else
+                args.out[(size_t)n * 2 * args.ldo + m] = v;
             }
           }
         }
