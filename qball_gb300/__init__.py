@@ -119,6 +119,8 @@ def _dev_ptr(x):
         return None
     if isinstance(x, int):
         return _P(x)
+    if hasattr(x, "is_contiguous") and not x.is_contiguous():
+        raise QbgError("device arrays must be contiguous (row-major [nst][ld] for states)")
     return _P(x.data_ptr())
 
 
