@@ -55,7 +55,9 @@ enum {
   QBG_PREC_MIXED_FFT64 = 2, /* as MIXED but FP64 transforms */
   QBG_PREC_MIXED_NL64 = 3,  /* as MIXED but FP64 projector GEMMs */
   QBG_PREC_MIXED_DF32 = 4   /* as MIXED but double-float (FP32 pair)
-                               transforms: ~48-bit, on the FP32 pipe */
+                               transforms: ~48-bit, on the FP32 pipe; the
+                               kinetic term and Taylor increment are
+                               double-float products added to FP64 */
 };
 
 typedef struct qbg_plan qbg_plan;
@@ -229,9 +231,11 @@ qbg_status qbg_set_selfconsistent(qbg_plan* plan, int on);
  * exponential of update (EhrenSampleStepper.cc:477-548); NULL means
  * "unchanged".  rho_mid (device double[N], may be NULL) receives the density
  * of the predicted psi(t+dt) built inside update() (ExponentialWavefunction-
- * Stepper.cc:259); nel (host, may be NULL) its electron count.  With
- * QBG_PREC_MIXED the three exponentials apply H in reduced precision and
- * accumulate the Taylor series in FP64. */
+ * Stepper.cc:259); nel (host, may be NULL) its electron count.  With a
+ * reduced-precision form the three exponentials apply H in that form and
+ * accumulate the Taylor series into the FP64 psi.  After
+ * qbg_set_selfconsistent(plan, 1) the local potential is rebuilt from the
+ * density of psi(t) before preupdate and from rho_mid before update. */
 qbg_status qbg_etrs_step(qbg_plan* plan, double* psi, int ld, int nst,
                          const double* occ, double dt, const double* A_t,
                          const double* A_tdt, double* rho_mid, double* nel,

@@ -86,15 +86,17 @@ __device__ __forceinline__ df32 df32_from_f64(double x) {
   }
   return df32(hi, lo);
 }
-// FP64 -> FP32 by truncating the significand to 24 bits (relative error
-// below 2^-23), from the bit pattern: no FP64 instruction.  |x| below 2^-126
-// gives zero.
-__device__ __forceinline__ float f32_trunc_from_f64(double x) {
+// FP64 -> FP32 rounded to nearest (ties away from zero) from the bit
+// pattern: half a unit of the 24-bit significand is added to the magnitude
+// bits before truncation (a carry into the exponent is the correct
+// rounding), so no FP64 instruction is issued.  |x| below 2^-126 gives zero.
+__device__ __forceinline__ float f32_from_f64_rn(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const int fe = (int)((b >> 52) & 0x7FF) - 1023 + 127;
+  const unsigned long long m = (b & 0x7FFFFFFFFFFFFFFFull) + (1ull << 28);
+  const int fe = (int)(m >> 52) - 1023 + 127;
   if (fe <= 0) return 0.f;
   return __uint_as_float(((unsigned)(b >> 32) & 0x80000000u) | ((unsigned)fe << 23) |
-                         (unsigned)((b >> 29) & 0x7FFFFF));
+                         (unsigned)((m >> 29) & 0x7FFFFF));
 }
 // FP32 -> FP64 from the bit pattern (exact for normal numbers; zero and
 // subnormal inputs give zero), no FP64 instruction

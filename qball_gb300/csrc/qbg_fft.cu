@@ -138,6 +138,23 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
   const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double2* os = out + (size_t)s * ldo;
+  if constexpr (MODE == 2) {
+    // scaled transform in the working type, in sphere order, for a separate
+    // (coalesced) epilogue pass
+    C* vs = reinterpret_cast<C*>(out) + (size_t)s * ldo;
+    for (int rl = warp; rl < nl; rl += nw) {
+      const RodInfo ri = rods[r0 + rl];
+      for (int i = lane; i < ri.size; i += 32) {
+        int z = ri.lmin + i;
+        if (z < 0) z += n2;
+        C vt = R[rl * ls + z];
+        vt.x *= scale;
+        vt.y *= scale;
+        vs[ri.first + i] = vt;
+      }
+    }
+    return;
+  }
   if constexpr (std::is_same<T, df32>::value && MODE == 1) {
     // double-float arithmetic; FP64 only for the add of each stored
     // component.  A lane loads all its coefficients of a rod (up to four)
@@ -219,6 +236,40 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
         }
       }
     }
+  }
+}
+
+// The H psi epilogue of the double-float form as its own pass over the
+// sphere (coalesced, one thread per coefficient): out = (o_nl + kin c) + v,
+// acc += fac out, with v the scaled forward transform stored by
+// k_z_fwd<df32, 2>.  Double-float arithmetic; FP64 only for the add that
+// forms each stored component.
+__global__ void __launch_bounds__(256)
+k_hpsi_epilogue_df32(const df32c* __restrict__ v, int ldv, const double2* psi, int ldp,
+                     double2* out, int ldo, int out_init, const double* __restrict__ kpg2,
+                     double2* acc, int lda, double2 fac, int ngw) {
+  // psi and acc may alias: each element is read before it is written by the
+  // same thread
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (g >= ngw) return;
+  const double2 c64 = psi[(size_t)s * ldp + g];
+  const double2 o0 = out_init ? out[(size_t)s * ldo + g] : make_double2(0.0, 0.0);
+  const double2 a0 = acc ? acc[(size_t)s * lda + g] : make_double2(0.0, 0.0);
+  const df32c vt = v[(size_t)s * ldv + g];
+  const df32 xk = df_scale2(df32_from_f64(kpg2[g]), 0.5f);
+  df32 ox = xk * df32_from_f64(c64.x), oy = xk * df32_from_f64(c64.y);
+  if (out_init) {
+    ox = ox + df32_from_f64(o0.x);
+    oy = oy + df32_from_f64(o0.y);
+  }
+  ox = ox + vt.x;
+  oy = oy + vt.y;
+  out[(size_t)s * ldo + g] = make_double2(f64_from_df32(ox), f64_from_df32(oy));
+  if (acc) {
+    const df32 fx = df32_from_f64(fac.x), fy = df32_from_f64(fac.y);
+    const df32 ix = fx * ox - fy * oy, iy = fx * oy + fy * ox;
+    acc[(size_t)s * lda + g] = make_double2(a0.x + f64_from_df32(ix), a0.y + f64_from_df32(iy));
   }
 }
 
@@ -413,6 +464,17 @@ k_sum_slots(const ST* __restrict__ slots, int nslots, long long n, double* __res
 // three-kernel path never leaves the SM.  Needs prime-factor lengths along
 // x and y that run in place, and the band rows plus one column group within
 // one CTA's shared memory.
+// the double-float H psi epilogue as a separate coalesced pass (1) or fused
+// into the forward z pass (0)
+#ifndef QBG_ZFWD_SPLIT
+#define QBG_ZFWD_SPLIT 1
+#endif
+constexpr bool kZfwdSplit = QBG_ZFWD_SPLIT != 0;
+#ifndef QBG_DENS_P3
+#define QBG_DENS_P3 0
+#endif
+constexpr bool kDensP3 = QBG_DENS_P3 != 0;
+
 // threads per CTA of the fused kernels: 768 for the three-pass 120-point
 // transforms (their codelets fit 80 registers), 512 for the two-pass ones
 #ifndef QBG_XYX_THREADS
@@ -649,9 +711,9 @@ k_xy_density(const cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ r
       W[cl * ls1 + y] = b >= 0 ? Xb[b * ls0 + c0 + cl] : czero<T>();
     }
     __syncthreads();
-    // (the y pass keeps the two-pass split here: with no forward half, its
-    // last pass writes straight to memory and measured faster)
-    if constexpr (kP3 && false) {
+    // (the y pass keeps the two-pass split by default: with no forward
+    // half, its last pass writes straight to memory)
+    if constexpr (kP3 && kDensP3) {
       pfa120_ab<+1>(W, ls1, gl);
       if (accumulate) {
         cp_async_wait_all();
@@ -1076,9 +1138,21 @@ qbg_status local_hpsi(qbg_plan* p, const double2* psi, int ld, double2* out, int
       QBG_TRY((run_y<T, Y_VLOC>(p, ns, nullptr, nullptr, nullptr, 0, st)));
       QBG_TRY(run_x<T>(p, false, ns, st));
     }
-    QBG_TRY((run_z_fwd<T, 1>(p, out + (size_t)s0 * ld, ld, ns, psi + (size_t)s0 * ld, ld,
-                             out_init ? 1 : 0, acc ? acc + (size_t)s0 * ldacc : nullptr, ldacc,
-                             fac, st)));
+    if (std::is_same<T, df32>::value && kZfwdSplit) {
+      QBG_TRY(ensure(&p->d_vsph, &p->vsph_bytes, sizeof(df32c) * (size_t)ch * p->ngw));
+      QBG_TRY((run_z_fwd<T, 2>(p, (double2*)p->d_vsph, p->ngw, ns, nullptr, 0, 0, nullptr, 0,
+                               fac, st)));
+      PhaseTimer pt(p, PH_Z_FWD, st);
+      k_hpsi_epilogue_df32<<<dim3((p->ngw + 255) / 256, ns), 256, 0, st>>>(
+          (const df32c*)p->d_vsph, p->ngw, psi + (size_t)s0 * ld, ld, out + (size_t)s0 * ld, ld,
+          out_init ? 1 : 0, p->d_kpg2A, acc ? acc + (size_t)s0 * ldacc : nullptr, ldacc, fac,
+          p->ngw);
+      QBG_LAUNCHED(p);
+    } else {
+      QBG_TRY((run_z_fwd<T, 1>(p, out + (size_t)s0 * ld, ld, ns, psi + (size_t)s0 * ld, ld,
+                               out_init ? 1 : 0, acc ? acc + (size_t)s0 * ldacc : nullptr, ldacc,
+                               fac, st)));
+    }
   }
   return QBG_OK;
 }

@@ -120,6 +120,7 @@ struct qbg_plan {
   double* d_red = nullptr; size_t red_bytes = 0;     // reduction partials
   double* d_rho = nullptr; size_t rho_bytes = 0;     // ETRS density scratch
   double* d_rho_slots = nullptr; size_t rho_slots_bytes = 0;  // [chunk][N] per-state density
+  void* d_vsph = nullptr; size_t vsph_bytes = 0;      // [chunk][ngw] forward transform (sphere)
   double* h_red = nullptr; size_t h_red_bytes = 0;   // pinned host copy
   // phase profiler (off unless qbg_profile(plan, 1))
   bool prof = false;

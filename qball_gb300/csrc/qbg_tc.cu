@@ -222,8 +222,8 @@ __global__ void k_split_rows4(const double2* __restrict__ x, int ld, int ncols,
   for (int j = 0; j < 4; ++j) {
     const int g = g0 + j;
     const double2 a = g < ncols ? x[(size_t)n * ld + g] : make_double2(0.0, 0.0);
-    const float xr = fscale ? f32_trunc_from_f64(a.x) * sf : __double2float_rn(a.x * sd);
-    const float xi = fscale ? f32_trunc_from_f64(a.y) * sf : __double2float_rn(a.y * sd);
+    const float xr = fscale ? f32_from_f64_rn(a.x) * sf : __double2float_rn(a.x * sd);
+    const float xi = fscale ? f32_from_f64_rn(a.y) * sf : __double2float_rn(a.y * sd);
     split2(xr, hi[2 * j], lo[2 * j]);
     split2(xi, hi[2 * j + 1], lo[2 * j + 1]);
   }
