@@ -241,6 +241,34 @@ qbg_status qbg_etrs_step(qbg_plan* plan, double* psi, int ld, int nst,
                          const double* A_tdt, double* rho_mid, double* nel,
                          void* stream);
 
+/* ---- Batched cells as one CUDA graph (no reference counterpart: the
+ *      reference steps one system per process group) -------------------- */
+typedef struct qbg_graph qbg_graph;
+/* Capture one ETRS step (qbg_etrs_step with A unchanged, no rho_mid/nel) of
+ * each of ncells independent cells -- distinct plans of any grid, basis, form
+ * and state count, psi[i] [ld[i] x nst[i]] with host occupations occ[i] --
+ * into one CUDA graph whose cells run as concurrent branches.  One
+ * uncaptured step runs first on scratch copies of the states (psi is not
+ * changed) so that the capture allocates and synchronises nothing; the
+ * occupations and vector potentials in force then must stay unchanged while
+ * the graph is used.  stream may be NULL (an internal stream captures). */
+qbg_status qbg_etrs_graph_create(int ncells, qbg_plan* const* plans,
+                                 double* const* psi, const int* ld,
+                                 const int* nst, const double* const* occ,
+                                 double dt, void* stream, qbg_graph** graph);
+/* one ETRS step of every cell (asynchronous on stream) */
+qbg_status qbg_etrs_graph_launch(qbg_graph* graph, void* stream);
+/* synchronise the device and read every cell's tensor-core status word
+ * (QBG_ERR_TIMEOUT if a bounded wait expired during a replay) */
+qbg_status qbg_etrs_graph_check(qbg_graph* graph);
+qbg_status qbg_etrs_graph_destroy(qbg_graph* graph);
+
+/* Autotuner: time H|psi> (two applications after a warm-up) for states per
+ * transform launch group in {8, 16, 32, 64} and keep the fastest for this
+ * plan; *chosen (may be NULL) receives it.  Synchronises. */
+qbg_status qbg_plan_autotune(qbg_plan* plan, const double* psi, int ld, int nst,
+                             const double* occ, void* stream, int* chosen);
+
 /* ---- Instrumentation (no reference counterpart beyond its TimerMap,
  *      NonLocalPotential.cc:54, EhrenSampleStepper.cc:1136-1149) ------- */
 /* Number of this library's kernel launches issued since plan creation. */

@@ -68,6 +68,11 @@ ABI = {
     "qbg_update_vhxc": [_P, _P, _P, _P],
     "qbg_set_selfconsistent": [_P, _I],
     "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
+    "qbg_etrs_graph_create": [_I, _P, _P, _P, _P, _P, _D, _P, _P],
+    "qbg_etrs_graph_launch": [_P, _P],
+    "qbg_etrs_graph_check": [_P],
+    "qbg_etrs_graph_destroy": [_P],
+    "qbg_plan_autotune": [_P, _P, _I, _I, _P, _P, _P],
     "qbg_launch_count": [_P, _P],
     "qbg_profile": [_P, _I],
     "qbg_profile_read": [_P, _P, _P, _I],
@@ -208,6 +213,16 @@ class FourierTransform:
         _check(lib().qbg_profile_read(self.h, _np_ptr(ms), _np_ptr(n), NPHASE), "qbg_profile_read")
         return {lib().qbg_phase_name(i).decode(): (float(ms[i]), int(n[i])) for i in range(NPHASE)}
 
+    def autotune(self, psi, occ, stream=None):
+        """Pick the states-per-launch-group that makes H|psi> fastest."""
+        o = np.ascontiguousarray(occ, np.float64)
+        ch = ctypes.c_int()
+        _check(lib().qbg_plan_autotune(self.h, _dev_ptr(psi), int(psi.shape[-1]),
+                                       int(psi.shape[0]), _np_ptr(o), _stream_ptr(stream),
+                                       ctypes.byref(ch)), "qbg_plan_autotune")
+        self.chunk = ch.value
+        return ch.value
+
     def set_chunk(self, n):
         _check(lib().qbg_plan_set_chunk(self.h, int(n)), "qbg_plan_set_chunk")
         self.chunk = int(n)
@@ -339,3 +354,43 @@ class Hamiltonian(FourierTransform):
                                    ctypes.byref(nel) if want_nel else None, _stream_ptr(stream)),
                "qbg_etrs_step")
         return nel.value if want_nel else None
+
+
+class EtrsGraph:
+    """One ETRS step of many independent cells captured as one CUDA graph.
+
+    cells: list of (Hamiltonian, psi device tensor [nst, ld], occ numpy).
+    Each Hamiltonian must be a distinct plan; psi tensors stay owned by the
+    caller and are advanced in place by every launch()."""
+
+    def __init__(self, cells, dt, stream=None):
+        n = len(cells)
+        self.cells = cells
+        self._plans = (_P * n)(*[c[0].h for c in cells])
+        self._psi = (_P * n)(*[_dev_ptr(c[1]) for c in cells])
+        self._ld = (ctypes.c_int * n)(*[int(c[1].shape[-1]) for c in cells])
+        self._nst = (ctypes.c_int * n)(*[int(c[1].shape[0]) for c in cells])
+        self._occ_arrays = [np.ascontiguousarray(c[2], np.float64) for c in cells]
+        self._occ = (_P * n)(*[_np_ptr(o) for o in self._occ_arrays])
+        g = _P()
+        _check(lib().qbg_etrs_graph_create(n, self._plans, self._psi, self._ld, self._nst,
+                                           self._occ, float(dt), _stream_ptr(stream),
+                                           ctypes.byref(g)), "qbg_etrs_graph_create")
+        self.h = g
+
+    def launch(self, stream=None):
+        _check(lib().qbg_etrs_graph_launch(self.h, _stream_ptr(stream)), "qbg_etrs_graph_launch")
+
+    def check(self):
+        _check(lib().qbg_etrs_graph_check(self.h), "qbg_etrs_graph_check")
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().qbg_etrs_graph_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,127 @@
+"""Many independent cells propagated together (the batched workload).
+
+    python -m qball_gb300.batch [--cells 64] [--steps 4] [--form mixed_df32]
+
+Seeded cells: edge L in [12, 24] bohr, cutoff 20-40 Ry, 4-64 atoms (s, p
+projectors), 8-256 states, each on one of the 32/48/64/96-point cubic grids
+that hold its basis (drawn at random).  Every cell gets its own plan, psi and
+vector-potential kick, and is stepped (a) one cell after another through
+qbg_etrs_step and (b) as one CUDA graph holding one ETRS step of every cell
+as concurrent branches (qbg_etrs_graph_*).  Before timing, each plan picks
+its states-per-launch-group with qbg_plan_autotune.  Prints one JSON line:
+aggregate cell-steps/s of both ways and the largest relative difference
+between their states.
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+GRIDS = (32, 48, 64, 96)
+
+
+def batch_cells(n, seed):
+    """(L, ecut Ha, grid, natoms, nst) for n seeded cells."""
+    import qball_gb300 as Q
+    rng = np.random.default_rng(seed)
+    out = []
+    while len(out) < n:
+        L = float(rng.uniform(12.0, 24.0))
+        ecut = float(rng.uniform(20.0, 40.0)) / 2.0
+        nst = int(rng.integers(8, 257))
+        natoms = int(min(rng.integers(4, 65), 0.3 * (L / 3.0) ** 3))
+        b = Q.Basis(L, ecut)
+        fit = [g for g in GRIDS if g >= max(b.np)]
+        if not fit:
+            continue
+        out.append((L, ecut, int(fit[rng.integers(0, len(fit))]), natoms, nst))
+    return out
+
+
+def main():
+    import torch
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cells", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=1)
+    ap.add_argument("--form", default="mixed_df32")
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--dt", type=float, default=0.05)
+    args = ap.parse_args()
+    torch.cuda.set_device(0)
+    specs = batch_cells(args.cells, args.seed)
+    A = synth.kick()
+    seq, bat = [], []
+    t0 = time.perf_counter()
+    for i, (L, ecut, g, natoms, nst) in enumerate(specs):
+        cell = synth.make_cell(None, seed=args.seed * 1000 + i, L=L, ecut=ecut, grid=(g, g, g),
+                               nst=nst, natoms=natoms, lmax=1)
+        b = Q.Basis(cell.L, cell.ecut)
+        psi = torch.from_numpy(synth.wavefunctions(cell, b)).cuda()
+        occ = synth.occupations(cell)
+        for dst in (seq, bat):
+            H = Q.Hamiltonian(b, *cell.grid, precision=args.form)
+            H.set_vlocal(synth.vlocal(cell))
+            H.set_nonlocal(synth.species(cell))
+            H.set_vector_potential(A)
+            dst.append((H, psi.clone(), occ))
+    for H, p, occ in seq + bat:
+        H.autotune(p, occ)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            for H, p, occ in seq:
+                H.etrs_step(p, occ, args.dt, stream=stream)
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            for H, p, occ in seq:
+                H.etrs_step(p, occ, args.dt, stream=stream)
+        e1.record(stream)
+        stream.synchronize()
+        ms_seq = e0.elapsed_time(e1)
+    graph = Q.EtrsGraph(bat, args.dt, stream=stream)
+    for _ in range(args.warmup):
+        graph.launch(stream=stream)
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        graph.launch(stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    graph.check()
+    ms_graph = e0.elapsed_time(e1)
+    diff = 0.0
+    for (_, ps, _), (_, pb, _) in zip(seq, bat):
+        d = (ps - pb).abs().pow(2).sum().sqrt() / ps.abs().pow(2).sum().sqrt()
+        diff = max(diff, float(d))
+    n = len(specs)
+    line = {
+        "workload": f"{n} seeded cells: L 12-24 bohr, 20-40 Ry, grids {list(GRIDS)}, 4-64 atoms "
+                    f"(s,p projectors), 8-256 states, delta kick, form {args.form}",
+        "cells": n, "states_total": int(sum(s[4] for s in specs)),
+        "grids": {str(g): sum(1 for s in specs if s[2] == g) for g in GRIDS},
+        "steps": args.steps, "warmup": args.warmup,
+        "cell_steps_per_s_graph": n * args.steps / (ms_graph / 1000.0),
+        "cell_steps_per_s_sequential": n * args.steps / (ms_seq / 1000.0),
+        "graph_speedup": ms_seq / ms_graph,
+        "max_rel_diff_graph_vs_sequential": diff,
+        "chunks": sorted({H.chunk for H, _, _ in bat}),
+        "setup_s": setup_s,
+        "device_gb_in_use": (lambda f: (f[1] - f[0]) / 1e9)(torch.cuda.mem_get_info()),
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

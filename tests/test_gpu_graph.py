@@ -1,0 +1,93 @@
+"""Batched cells stepped as one CUDA graph, and the chunk autotuner.
+
+A graph replay must give the same states as stepping every cell on its own
+(same kernels in the same order per cell: bitwise, checked to 1e-13), for
+cells of different grids, forms and state counts, with and without the
+self-consistent potential; the autotuner must keep H|psi> unchanged.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+import qball_gb300 as Q
+from qball_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def dev(x):
+    return _torch().from_numpy(np.ascontiguousarray(x)).to("cuda:0")
+
+
+def make(name, prec, hxc=False, **kw):
+    cell = synth.make_cell(name, **kw)
+    b = Q.Basis(cell.L, cell.ecut)
+    H = Q.Hamiltonian(b, *cell.grid, precision=prec)
+    H.set_vlocal(synth.vlocal(cell))
+    H.set_nonlocal(synth.species(cell))
+    H.set_vector_potential(synth.kick())
+    psi = synth.wavefunctions(cell, b)
+    occ = synth.occupations(cell)
+    if hxc:
+        vb = Q.Basis(cell.L, synth.density_ecut(cell))
+        H.set_density_basis(vb)
+        vion, rhopst = synth.ionic_terms(cell, vb)
+        H.set_ionic_terms(vion, rhopst)
+        torch = _torch()
+        rho = torch.zeros(H.n012, dtype=torch.float64, device="cuda:0")
+        H.update_density(dev(psi), occ, rho)
+        H.update_vhxc(rho)
+        H.set_selfconsistent(True)
+    return H, psi, occ
+
+
+CELLS = [("t12", "fp64", False, {}), ("t12b", "mixed_df32", False, {}),
+         ("c1", "mixed_df32", False, {"nst": 8}), ("t12", "mixed", True, {"grid": (40, 40, 40)})]
+
+
+def test_graph_replay_matches_individual_steps(cuda):
+    torch = _torch()
+    ref, bat = [], []
+    for name, prec, hxc, kw in CELLS:
+        H1, psi, occ = make(name, prec, hxc, **kw)
+        H2, _, _ = make(name, prec, hxc, **kw)
+        ref.append((H1, dev(psi), occ))
+        bat.append((H2, dev(psi), occ))
+    dt = 0.05
+    stream = torch.cuda.Stream()
+    g = Q.EtrsGraph(bat, dt, stream=stream)
+    for _ in range(2):
+        g.launch(stream=stream)
+    g.check()
+    for H, p, occ in ref:
+        for _ in range(2):
+            H.etrs_step(p, occ, dt)
+    torch.cuda.synchronize()
+    for (_, pr, _), (_, pb, _) in zip(ref, bat):
+        assert rel_err(pb.cpu().numpy(), pr.cpu().numpy()) < 1e-13
+    g.close()
+
+
+def test_graph_rejects_repeated_plan(cuda):
+    H, psi, occ = make("t12", "fp64")
+    p = dev(psi)
+    with pytest.raises(Q.QbgError, match="repeats"):
+        Q.EtrsGraph([(H, p, occ), (H, p, occ)], 0.05)
+
+
+def test_autotune_keeps_hpsi(cuda):
+    torch = _torch()
+    H, psi, occ = make("c1", "mixed_df32")
+    p = dev(psi)
+    before = torch.zeros_like(p)
+    H.hpsi(p, before, occ)
+    ch = H.autotune(p, occ)
+    assert ch in (8, 16, 32, 64)
+    after = torch.zeros_like(p)
+    H.hpsi(p, after, occ)
+    assert rel_err(after.cpu().numpy(), before.cpu().numpy()) < 1e-12
