@@ -546,7 +546,8 @@ def run_ours(args, rank, world, local):
                 "form": args.form, "form_desc": form_desc.get(args.form, args.form),
                 "dipole_rel_err_200_steps": acc.get(args.form),
                 "data": "synthetic (seeded cell, random orthonormal states)",
-                "config": {"workload": f"{args.config}: 216 atoms, L=30 bohr, ecut 50 Ry, grid "
+                "config": {"workload": f"{args.config}: {cell.natoms} atoms, L={cell.L:g} bohr, "
+                                       f"ecut {2 * cell.ecut:g} Ry, grid "
                                        f"{cell.grid[0]}^3, {basis.ngw} PW (full sphere), "
                                        f"{cell.nst} states, {nproj_of(cell)} KB projectors, "
                                        f"ETRS dt={args.dt}, delta kick A_z=0.01",
@@ -555,7 +556,8 @@ def run_ours(args, rank, world, local):
                                            f"psi(t+dt) every step, density sphere "
                                            f"{2 * vb.ecut:g} Ry ({vb.ngw} G)" if hxc else
                                            "fixed local potential"),
-                           "l2": "inputs (psi 1.1 GB) larger than L2; no flush",
+                           "l2": f"inputs (psi {psi.numel() * 16 / 1e9:.1f} GB) larger than L2; "
+                                 "no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
                 "gpu_launches": launches, "clocks": clk, "roofline": roofline,
                 "e2e": e2e, "other_forms": others, "cpu_baseline": cpu}

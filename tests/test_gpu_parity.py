@@ -73,11 +73,12 @@ def test_fft_backward_forward_vs_reference_golden(cuda, name):
                                          (20.0, 10.0, (48, 48, 48)), (10.0, 6.0, (28, 28, 28)),
                                          (10.0, 6.0, (22, 22, 26)),
                                          (12.0, 10.0, (120, 48, 40)),
-                                         (12.0, 10.0, (72, 80, 144))])
+                                         (12.0, 10.0, (72, 80, 144)),
+                                         (12.0, 10.0, (160, 36, 50))])
 def test_fft_vs_oracle_many_grids(cuda, L, ecut, grid):
     """radix 2,3,4,5,8, the direct-DFT primes 7, 11 and 13, and the
     prime-factor lengths 120 = 8x15, 48 = 16x3, 40 = 8x5, 72 = 8x9,
-    80 = 16x5, 144 = 16x9"""
+    80 = 16x5, 144 = 16x9, and 160 (the 512-atom cell's length, Stockham)"""
     b = Q.Basis(L, ecut)
     ob = O.Basis(b.a, ecut)
     oft = O.FT(ob, *grid)
