@@ -269,6 +269,12 @@ qbg_status qbg_etrs_graph_destroy(qbg_graph* graph);
 qbg_status qbg_plan_autotune(qbg_plan* plan, const double* psi, int ld, int nst,
                              const double* occ, void* stream, int* chosen);
 
+/* Diagnostic, no reference counterpart: runs one bounded mbarrier wait that
+ * nothing completes (polls polls, 1..2^20) and returns QBG_ERR_TIMEOUT when
+ * it gives up as designed -- the path every wait of the tensor-core kernel
+ * takes instead of hanging.  The device stays usable.  Synchronises. */
+qbg_status qbg_selftest_wait_timeout(int polls);
+
 /* ---- Instrumentation (no reference counterpart beyond its TimerMap,
  *      NonLocalPotential.cc:54, EhrenSampleStepper.cc:1136-1149) ------- */
 /* Number of this library's kernel launches issued since plan creation. */

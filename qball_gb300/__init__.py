@@ -73,6 +73,7 @@ ABI = {
     "qbg_etrs_graph_check": [_P],
     "qbg_etrs_graph_destroy": [_P],
     "qbg_plan_autotune": [_P, _P, _I, _I, _P, _P, _P],
+    "qbg_selftest_wait_timeout": [_I],
     "qbg_launch_count": [_P, _P],
     "qbg_profile": [_P, _I],
     "qbg_profile_read": [_P, _P, _P, _I],
@@ -354,6 +355,11 @@ class Hamiltonian(FourierTransform):
                                    ctypes.byref(nel) if want_nel else None, _stream_ptr(stream)),
                "qbg_etrs_step")
         return nel.value if want_nel else None
+
+
+def selftest_wait_timeout(polls=20000):
+    """Run one bounded device wait that must expire; returns the status."""
+    return int(lib().qbg_selftest_wait_timeout(int(polls)))
 
 
 class EtrsGraph:

@@ -247,8 +247,9 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
 }
 // bounded wait for the phase with parity `par` to complete; false on timeout
 // or when another CTA has already raised the grid-wide error word
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, const int* gstatus) {
-  for (int it = 0; it < TC_SPIN; ++it) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, const int* gstatus,
+                                          int limit = TC_SPIN) {
+  for (int it = 0; it < limit; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -758,6 +759,18 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
   return QBG_OK;
 }
 
+// Diagnostic: one thread waits on an mbarrier that nothing completes, with
+// `polls` polls; the wait must give up and report through the status word,
+// leaving the context usable (the same bounded wait the GEMM's roles use).
+__global__ void k_wait_selftest(int polls, int* status) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (!mbar_wait(&bar, 0, status, polls)) atomicExch(status, 1);
+  }
+}
+
 qbg_status tc_check_status(qbg_plan* p) {
   TcTables* t = (TcTables*)p->tc;
   if (!t) return QBG_OK;
@@ -772,3 +785,25 @@ qbg_status tc_check_status(qbg_plan* p) {
 }
 
 }  // namespace qbg
+
+extern "C" qbg_status qbg_selftest_wait_timeout(int polls) {
+  using namespace qbg;
+  if (polls < 1 || polls > (1 << 20)) {
+    set_error("qbg_selftest_wait_timeout: polls must be in [1, 2^20]");
+    return QBG_ERR_INVALID;
+  }
+  int* d = nullptr;
+  QBG_CUDA(cudaMalloc(&d, sizeof(int)));
+  cudaMemset(d, 0, sizeof(int));
+  k_wait_selftest<<<1, 32>>>(polls, d);
+  cudaError_t e = cudaGetLastError();
+  int h = 0;
+  if (e == cudaSuccess) e = cudaMemcpy(&h, d, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_status(e, "qbg_selftest_wait_timeout");
+  if (h) {
+    set_error("bounded wait expired after %d polls (self-test)", polls);
+    return QBG_ERR_TIMEOUT;
+  }
+  return QBG_OK;
+}

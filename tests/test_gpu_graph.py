@@ -91,3 +91,17 @@ def test_autotune_keeps_hpsi(cuda):
     after = torch.zeros_like(p)
     H.hpsi(p, after, occ)
     assert rel_err(after.cpu().numpy(), before.cpu().numpy()) < 1e-12
+
+
+def test_bounded_wait_expires_and_context_survives(cuda):
+    """A device wait on a barrier that nothing completes gives up after its
+    poll limit with QBG_ERR_TIMEOUT (no hang, no fault); the GPU keeps
+    working afterwards."""
+    assert Q.selftest_wait_timeout(20000) == 5  # QBG_ERR_TIMEOUT
+    assert "bounded wait expired" in Q.lib().qbg_last_error().decode()
+    torch = _torch()
+    H, psi, occ = make("t12", "fp64")
+    out = torch.zeros_like(dev(psi))
+    H.hpsi(dev(psi), out, occ)
+    torch.cuda.synchronize()
+    assert torch.isfinite(out.abs()).all()
