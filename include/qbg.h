@@ -241,6 +241,60 @@ qbg_status qbg_etrs_step(qbg_plan* plan, double* psi, int ld, int nst,
                          const double* A_tdt, double* rho_mid, double* nel,
                          void* stream);
 
+/* ---- Adjoint of the ETRS step (no reference counterpart: the reference
+ *      propagates forward only; the step differentiated is that of
+ *      ExponentialWavefunctionStepper.cc:153-276 with a fixed local
+ *      potential, i.e. qbg_etrs_step without qbg_set_selfconsistent) ----- */
+/* One step psi_{n+1} = P(H(A_{n+1})) P(H(A_n)) psi_n, P = 4th-order Taylor
+ * polynomial of exp(-i H dt/2), taken backwards.  With the adjoint state
+ * lambda defined by dL = 2 Re sum_s <lambda_s|d psi_s>:
+ *   lambda (device [ld x nst], in: lambda_{n+1}) <- P_a^+ P_b^+ lambda;
+ *   grad_v (device double[N], may be NULL) += dL/dv(r) of the plan's local
+ *     potential on the grid points, through this step;
+ *   grad_a (host double[2], may be NULL) += dL/da_n, dL/da_{n+1}: the
+ *     derivatives along the unit direction e (host double[3]) of the vector
+ *     potential, through the kinetic term |k+G-A|^2/2 and the projectors
+ *     beta(k+G-A) (NonLocalPotential.cc:1962-2037).
+ * psi_n: device state at t_n; phi_n: device half step P(H(A_n)) psi_n or
+ * NULL (then recomputed, four more H applications).  A_n, A_np1: host
+ * double[3] or NULL (keep the plan's A); the plan is left at A_n.  occ is
+ * not used (reserved).  Costs 14 H applications, 16 backward transforms and,
+ * with grad_a, 32 projections on the projector tables and their derivative
+ * along e.  Synchronises when grad_a is given. */
+qbg_status qbg_etrs_adjoint_step(qbg_plan* plan, const double* psi_n,
+                                 const double* phi_n, int ld, int nst,
+                                 const double* occ, double dt,
+                                 const double* A_n, const double* A_np1,
+                                 const double* e, double* lambda,
+                                 double* grad_v, double* grad_a, void* stream);
+
+/* Checkpointed forward/backward operator pair over nsteps fixed-potential
+ * ETRS steps (nsteps >= 1) with a per-step vector potential (laser field in
+ * the velocity gauge, VectorPotential.h:150-160).  The forward pass keeps
+ * psi every K steps in device memory (ceil(nsteps/K) copies); the backward
+ * pass recomputes each segment of K steps from its checkpoint (keeping
+ * psi_n and the half steps of that segment, 2K copies) and runs the adjoint
+ * steps in reverse. */
+typedef struct qbg_td qbg_td;
+qbg_status qbg_td_create(qbg_plan* plan, int ld, int nst, const double* occ,
+                         double dt, int nsteps, int K, qbg_td** td);
+/* psi (device [ld x nst]): psi_0 in, psi_nsteps out.  A: host double
+ * [(nsteps+1) x 3], A_n at t_n.  J (host double[(nsteps+1) x 3] or NULL):
+ * the total current of every psi_n at A_n, as qbg_current with nel = sum occ.
+ * Synchronises. */
+qbg_status qbg_td_forward(qbg_td* td, double* psi, const double* A, double* J,
+                          void* stream);
+/* Gradients of a loss L(J_0..J_nsteps) given dLdJ (host double[(nsteps+1)
+ * x 3]): grad_v (device double[N] or NULL) = dL/dv(r); grad_a (host double
+ * [nsteps+1] or NULL) = dL/da_n along e (host double[3], required with
+ * grad_a), including the explicit A_n nel term of J_n; lambda0 (device
+ * [ld x nst] or NULL) = the adjoint state of psi_0.  Needs a forward pass.
+ * Synchronises. */
+qbg_status qbg_td_backward(qbg_td* td, const double* dLdJ, const double* e,
+                           double* grad_v, double* grad_a, double* lambda0,
+                           void* stream);
+qbg_status qbg_td_destroy(qbg_td* td);
+
 /* ---- Batched cells as one CUDA graph (no reference counterpart: the
  *      reference steps one system per process group) -------------------- */
 typedef struct qbg_graph qbg_graph;

@@ -68,6 +68,11 @@ ABI = {
     "qbg_update_vhxc": [_P, _P, _P, _P],
     "qbg_set_selfconsistent": [_P, _I],
     "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
+    "qbg_etrs_adjoint_step": [_P, _P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P],
+    "qbg_td_create": [_P, _I, _I, _P, _D, _I, _I, _P],
+    "qbg_td_forward": [_P, _P, _P, _P, _P],
+    "qbg_td_backward": [_P, _P, _P, _P, _P, _P, _P],
+    "qbg_td_destroy": [_P],
     "qbg_etrs_graph_create": [_I, _P, _P, _P, _P, _P, _D, _P, _P],
     "qbg_etrs_graph_launch": [_P, _P],
     "qbg_etrs_graph_check": [_P],
@@ -355,6 +360,70 @@ class Hamiltonian(FourierTransform):
                                    ctypes.byref(nel) if want_nel else None, _stream_ptr(stream)),
                "qbg_etrs_step")
         return nel.value if want_nel else None
+
+    def etrs_adjoint_step(self, psi_n, lam, dt, A_n=None, A_np1=None, e=None, grad_v=None,
+                          want_grad_a=False, phi_n=None, stream=None):
+        """lam <- (adjoint of one fixed-potential ETRS step) lam; grad_v
+        (device, N doubles) accumulates dL/dv(r); returns [dL/da_n,
+        dL/da_{n+1}] along e when want_grad_a."""
+        n, ldv = psi_n.shape[0], psi_n.shape[-1]
+        an = np.ascontiguousarray(A_n, np.float64) if A_n is not None else None
+        anp = np.ascontiguousarray(A_np1, np.float64) if A_np1 is not None else None
+        ev = np.ascontiguousarray(e, np.float64) if e is not None else None
+        ga = np.zeros(2) if want_grad_a else None
+        _check(lib().qbg_etrs_adjoint_step(self.h, _dev_ptr(psi_n), _dev_ptr(phi_n), ldv, n, None,
+                                           float(dt), _np_ptr(an), _np_ptr(anp), _np_ptr(ev),
+                                           _dev_ptr(lam), _dev_ptr(grad_v), _np_ptr(ga),
+                                           _stream_ptr(stream)), "qbg_etrs_adjoint_step")
+        return ga
+
+
+class TDPropagation:
+    """Checkpointed forward/backward operator pair over nsteps fixed-potential
+    ETRS steps of one plan (qbg_td_*): forward() propagates psi in place
+    under a per-step vector potential A[n] and returns the current J[n];
+    backward(dLdJ) returns the gradients of a loss of the currents with
+    respect to v(r) and to the vector potential along a direction e."""
+
+    def __init__(self, H, psi, occ, dt, nsteps, K=20):
+        self.H = H
+        self.nst, self.ld = int(psi.shape[0]), int(psi.shape[-1])
+        self.nsteps = int(nsteps)
+        self._occ = np.ascontiguousarray(occ, np.float64)
+        h = _P()
+        _check(lib().qbg_td_create(H.h, self.ld, self.nst, _np_ptr(self._occ), float(dt),
+                                   self.nsteps, int(K), ctypes.byref(h)), "qbg_td_create")
+        self.h = h
+
+    def forward(self, psi, A, stream=None):
+        A = np.ascontiguousarray(np.broadcast_to(np.asarray(A, np.float64),
+                                                 (self.nsteps + 1, 3)))
+        J = np.zeros((self.nsteps + 1, 3))
+        _check(lib().qbg_td_forward(self.h, _dev_ptr(psi), _np_ptr(A), _np_ptr(J),
+                                    _stream_ptr(stream)), "qbg_td_forward")
+        return J
+
+    def backward(self, dLdJ, e=None, grad_v=None, lambda0=None, stream=None):
+        """grad_v: device array of N doubles (overwritten) or None; returns
+        dL/da_n along e (numpy, nsteps+1) when e is given, else None."""
+        g = np.ascontiguousarray(dLdJ, np.float64).reshape(self.nsteps + 1, 3)
+        ev = np.ascontiguousarray(e, np.float64) if e is not None else None
+        ga = np.zeros(self.nsteps + 1) if e is not None else None
+        _check(lib().qbg_td_backward(self.h, _np_ptr(g), _np_ptr(ev), _dev_ptr(grad_v),
+                                     _np_ptr(ga), _dev_ptr(lambda0), _stream_ptr(stream)),
+               "qbg_td_backward")
+        return ga
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().qbg_td_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def selftest_wait_timeout(polls=20000):

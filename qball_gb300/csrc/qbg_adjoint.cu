@@ -1,0 +1,595 @@
+// qbg_adjoint.cu -- adjoint of the fixed-potential ETRS step and the
+// checkpointed forward/backward operator pair built on it.
+//
+// Forward step n (ExponentialWavefunctionStepper.cc:153-276 without the
+// density-dependent Hamiltonian): psi_{n+1} = P_b P_a psi_n with
+// P(H, tau) = sum_{k<=4} c_k H^k, c_k = (-i tau)^k / k!, tau = dt/2,
+// P_a = P(H(A_n)), P_b = P(H(A_{n+1})).  With the adjoint state defined by
+// dL = 2 Re sum_s <lambda_s|d psi_s>, and H Hermitian:
+//   lambda_n = P_a^+ P_b^+ lambda_{n+1} + dL/dpsi_n*,   P^+ = sum conj(c_k) H^k.
+// A parameter theta of H enters through dP = sum_k c_k sum_{j+m=k-1}
+// H^j dH H^m, so for one factor applied to x0 with adjoint y0
+//   dL/dtheta = 2 Re sum_s sum_{m<=3} <M_m|dH/dtheta|H^m x0>,
+//   M_m = sum_{j<=3-m} conj(c_{j+m+1}) H^j y0.
+// For the local potential dH/dv(r) is the real-space multiplication, so
+//   dL/dv(r) = (2/N) Re sum_s sum_m conj(M_m(r)) (H^m x0)(r)
+// (backward transforms of M_m and H^m x0, FourierTransform's conventions).
+// For the vector potential along e (A = A0 + a e), the kinetic term gives
+// dH/da = -(k+G-A).e and the projectors V = sum_p |b_p> D_p/Omega <b_p| give
+//   <M|dV/da|X> = sum_p D_p/Omega (conj(<b'_p|M>) <b_p|X> + conj(<b_p|M>) <b'_p|X>)
+// with b' = db/da from k_anl_da.  Each factor costs 7 H applications
+// (H^1..3 x0, H^1..4 y0), 8 backward transforms and 16 projections.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "qbg_internal.h"
+
+namespace qbg {
+
+#define QBG_TRY(x)                \
+  do {                            \
+    qbg_status s_ = (x);          \
+    if (s_ != QBG_OK) return s_;  \
+  } while (0)
+
+struct AdjWork {
+  size_t vec_bytes = 0;          // one [ld x nst] complex FP64 block
+  double2* X[3] = {};            // H^m x0, m = 1..3
+  double2* Y[4] = {};            // H^j y0, j = 1..4; then M_m in Y[3-m]
+  double2* chi = nullptr;        // P_b^+ lambda
+  double2* phi = nullptr; size_t phi_bytes = 0;  // P_a psi_n when the caller gives none
+  double2* fields = nullptr; size_t fields_bytes = 0;  // [8][chunk][N] real space
+  double2* proj = nullptr; size_t proj_bytes = 0;      // [16][nst][P]
+  double* part = nullptr; size_t part_bytes = 0;       // block partial sums
+  double* occ = nullptr; size_t occ_bytes = 0;         // per-state occupations
+  std::vector<double> h_part;
+  // derivative projector table for (A, e)
+  double2* dbeta = nullptr; size_t dbeta_bytes = 0;
+  void* dproj = nullptr;
+  double dA[3] = {0, 0, 0}, de[3] = {0, 0, 0};
+  bool dvalid = false;
+};
+
+static void work_free(AdjWork* w) {
+  if (!w) return;
+  void* bufs[] = {w->X[0], w->X[1], w->X[2], w->Y[0], w->Y[1], w->Y[2], w->Y[3], w->chi, w->phi,
+                  w->fields, w->proj, w->part, w->occ, w->dbeta};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  tc_proj_free(w->dproj);
+  delete w;
+}
+
+void adj_release(qbg_plan* p) {
+  work_free((AdjWork*)p->adj);
+  p->adj = nullptr;
+}
+
+static AdjWork* work_of(qbg_plan* p) {
+  if (!p->adj) p->adj = new AdjWork;
+  return (AdjWork*)p->adj;
+}
+
+static qbg_status work_vectors(AdjWork* w, size_t bytes) {
+  if (w->vec_bytes >= bytes && w->chi) return QBG_OK;
+  double2** all[] = {&w->X[0], &w->X[1], &w->X[2], &w->Y[0], &w->Y[1], &w->Y[2], &w->Y[3],
+                     &w->chi};
+  size_t cur = 0;
+  for (double2** b : all) {
+    size_t c = w->vec_bytes;
+    QBG_TRY(ensure((void**)b, &c, bytes));
+    cur = c;
+  }
+  w->vec_bytes = cur;
+  return QBG_OK;
+}
+
+// ------------------------------------------------------------------ kernels
+struct Comb {
+  const double2* in[5];
+  double2 c[5];
+  int n;
+};
+
+// out[s][g] = sum_k c_k in_k[s][g]
+__global__ void k_comb(Comb cb, int ld, int ngw, double2* __restrict__ out) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (g >= ngw) return;
+  const size_t o = (size_t)s * ld + g;
+  double re = 0.0, im = 0.0;
+  for (int k = 0; k < cb.n; ++k) {
+    const double2 v = cb.in[k][o];
+    re += cb.c[k].x * v.x - cb.c[k].y * v.y;
+    im += cb.c[k].x * v.y + cb.c[k].y * v.x;
+  }
+  out[o] = make_double2(re, im);
+}
+
+// lam[s][g] += -occ_s (gJ . (k+G)) psi[s][g]: dL/dpsi* of L(J) through
+// J_d = -sum_s occ_s sum_G (k+G)_d |c_sG|^2 + A_d nel (CurrentDensity.cc:39-106)
+__global__ void k_direct(const double2* __restrict__ psi, int ld, int ngw,
+                         const double* __restrict__ kpgx, const double* __restrict__ occ,
+                         double g0, double g1, double g2, double2* __restrict__ lam) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  if (g >= ngw) return;
+  const double f = -occ[s] * (g0 * kpgx[g] + g1 * kpgx[ngw + g] + g2 * kpgx[2 * ngw + g]);
+  const size_t o = (size_t)s * ld + g;
+  const double2 v = psi[o];
+  double2 l = lam[o];
+  l.x += f * v.x;
+  l.y += f * v.y;
+  lam[o] = l;
+}
+
+struct Quad {
+  const double2* M[4];
+  const double2* X[4];
+};
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int k = blockDim.x / 2; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) red[threadIdx.x] += red[threadIdx.x + k];
+    __syncthreads();
+  }
+  return red[0];
+}
+
+// kinetic part of dL/da: part[s*gridDim.x + b] = sum_{g in block b} sum_m
+//   Re(conj(M_m) X_m) * (-(k+G-A).e)
+__global__ void __launch_bounds__(256)
+k_grad_kin(Quad q, int ld, int ngw, const double* __restrict__ kpgx, double A0, double A1,
+           double A2, double e0, double e1, double e2, double* __restrict__ part) {
+  __shared__ double red[256];
+  const int s = blockIdx.y;
+  double acc = 0.0;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ngw; g += gridDim.x * blockDim.x) {
+    const size_t o = (size_t)s * ld + g;
+    double t = 0.0;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const double2 a = q.M[m][o], b = q.X[m][o];
+      t += a.x * b.x + a.y * b.y;
+    }
+    const double d = -((kpgx[g] - A0) * e0 + (kpgx[ngw + g] - A1) * e1 +
+                       (kpgx[2 * ngw + g] - A2) * e2);
+    acc += t * d;
+  }
+  const double r = block_sum(acc, red);
+  if (threadIdx.x == 0) part[(size_t)s * gridDim.x + blockIdx.x] = r;
+}
+
+// nonlocal part of dL/da from the projections pr[v][s][p]: v = m (<b|M_m>),
+// 4+m (<b|X_m>), 8+m (<b'|M_m>), 12+m (<b'|X_m>)
+__global__ void __launch_bounds__(256)
+k_grad_nl(const double2* __restrict__ pr, int nst, int P, const double* __restrict__ wt,
+          double* __restrict__ part) {
+  __shared__ double red[256];
+  const size_t total = (size_t)nst * P;
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (i < total) {
+    const int p = (int)(i % P);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const double2 bm = pr[(size_t)m * total + i], bx = pr[(size_t)(4 + m) * total + i];
+      const double2 dm = pr[(size_t)(8 + m) * total + i], dx = pr[(size_t)(12 + m) * total + i];
+      acc += (dm.x * bx.x + dm.y * bx.y) + (bm.x * dx.x + bm.y * dx.y);
+    }
+    acc *= wt[p];
+  }
+  const double r = block_sum(acc, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+// grad[r] += scale * sum_{s<ns} sum_m Re(conj(F[m][s][r]) F[4+m][s][r]);
+// fields F: [8][ns][N]; one writer per grid point
+__global__ void k_grad_v(const double2* __restrict__ F, int ns, long long N, double scale,
+                         double* __restrict__ grad) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const size_t fs = (size_t)ns * N;
+  double acc = 0.0;
+  for (int s = 0; s < ns; ++s) {
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      const double2 a = F[(size_t)m * fs + (size_t)s * N + r];
+      const double2 b = F[(size_t)(4 + m) * fs + (size_t)s * N + r];
+      acc += a.x * b.x + a.y * b.y;
+    }
+  }
+  grad[r] += scale * acc;
+}
+
+// ------------------------------------------------------------- host side
+// backward transform in the plan's transform arithmetic
+static qbg_status field_bwd(qbg_plan* p, const double2* c, int ld, double2* f, int nb,
+                            cudaStream_t st) {
+  switch (p->prec) {
+    case QBG_PREC_FP64:
+    case QBG_PREC_MIXED_FFT64: return backward<double>(p, c, ld, f, nb, st);
+    case QBG_PREC_MIXED_DF32: return backward<df32>(p, c, ld, f, nb, st);
+    default: return backward<float>(p, c, ld, f, nb, st);
+  }
+}
+
+// derivative projector table for the plan's current A and direction e
+static qbg_status ensure_dtable(qbg_plan* p, AdjWork* w, const double* e, cudaStream_t st) {
+  if (p->nproj == 0) return QBG_OK;
+  if (w->dvalid && !memcmp(w->dA, p->A, sizeof(w->dA)) && !memcmp(w->de, e, sizeof(w->de)))
+    return QBG_OK;
+  w->dvalid = false;
+  QBG_TRY(ensure((void**)&w->dbeta, &w->dbeta_bytes, sizeof(double2) * (size_t)p->nproj * p->ngw));
+  QBG_TRY(nl_build_da(p, e, w->dbeta, st));
+  if (uses_tc(p)) {
+    tc_proj_free(w->dproj);
+    w->dproj = nullptr;
+    QBG_TRY(tc_proj_build(p, w->dbeta, &w->dproj, st));
+  }
+  memcpy(w->dA, p->A, sizeof(w->dA));
+  memcpy(w->de, e, sizeof(w->de));
+  w->dvalid = true;
+  return QBG_OK;
+}
+
+static qbg_status project(qbg_plan* p, AdjWork* w, bool deriv, const double2* x, int ld,
+                          int nst, double2* f, cudaStream_t st) {
+  if (uses_tc(p)) return tc_project(p, deriv ? w->dproj : nullptr, x, ld, nst, f, st);
+  return nl_project64(p, deriv ? w->dbeta : p->d_anl, x, ld, nst, f, st);
+}
+
+static qbg_status comb(qbg_plan* p, const double2* const* in, const double2* c, int n, int ld,
+                       int nst, double2* out, cudaStream_t st) {
+  Comb cb;
+  for (int k = 0; k < 5; ++k) {
+    cb.in[k] = k < n ? in[k] : nullptr;
+    cb.c[k] = k < n ? c[k] : make_double2(0.0, 0.0);
+  }
+  cb.n = n;
+  k_comb<<<dim3((p->ngw + 255) / 256, nst), 256, 0, st>>>(cb, ld, p->ngw, out);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+static qbg_status sum_part(qbg_plan* p, AdjWork* w, size_t n, double* out, cudaStream_t st) {
+  w->h_part.resize(n);
+  QBG_CUDA(cudaMemcpyAsync(w->h_part.data(), w->part, sizeof(double) * n, cudaMemcpyDeviceToHost,
+                           st));
+  QBG_CUDA(cudaStreamSynchronize(st));
+  double s = 0.0;
+  for (size_t i = 0; i < n; ++i) s += w->h_part[i];
+  *out = s;
+  (void)p;
+  return QBG_OK;
+}
+
+// One Taylor factor P(H(A)) of the step, with the plan's A already set:
+// y_next = P^+ y0; grad_v (device, may be null) += dL/dv and *ga (may be
+// null) += dL/da along e, for the factor that the forward applied to x0.
+static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* x0, const double2* y0,
+                             double2* y_next, int ld, int nst, const double* d_occ, double tau,
+                             const double* e, double* grad_v, double* ga, cudaStream_t st) {
+  const double2 zero = make_double2(0.0, 0.0);
+  // c_k = (-i tau)^k / k! by the recursion of the forward (factor *= -i tau / k)
+  double2 c[5];
+  c[0] = make_double2(1.0, 0.0);
+  for (int k = 1; k <= 4; ++k) {
+    const double m_re = -0.0 * tau / (double)k, m_im = -1.0 * tau / (double)k;
+    c[k] = make_double2(c[k - 1].x * m_re - c[k - 1].y * m_im, c[k - 1].x * m_im + c[k - 1].y * m_re);
+  }
+  double2 cc[5];
+  for (int k = 0; k <= 4; ++k) cc[k] = make_double2(c[k].x, -c[k].y);
+  int nb = 0;
+  const double2* xv[4] = {x0, w->X[0], w->X[1], w->X[2]};
+  for (int m = 1; m <= 3; ++m)
+    QBG_TRY(hpsi_core(p, xv[m - 1], ld, w->X[m - 1], nst, d_occ, nullptr, &nb, nullptr, 0, zero, st));
+  const double2* yv[5] = {y0, w->Y[0], w->Y[1], w->Y[2], w->Y[3]};
+  for (int j = 1; j <= 4; ++j)
+    QBG_TRY(hpsi_core(p, yv[j - 1], ld, w->Y[j - 1], nst, d_occ, nullptr, &nb, nullptr, 0, zero, st));
+  QBG_TRY(comb(p, yv, cc, 5, ld, nst, y_next, st));
+  if (!grad_v && !ga) return QBG_OK;
+  // M_m = sum_{j<=3-m} conj(c_{j+m+1}) H^j y0 into Y[3-m] (each written after its last read)
+  for (int m = 0; m <= 3; ++m) {
+    double2 cm[4];
+    for (int j = 0; j <= 3 - m; ++j) cm[j] = cc[j + m + 1];
+    QBG_TRY(comb(p, yv, cm, 4 - m, ld, nst, w->Y[3 - m], st));
+  }
+  const double2* M[4] = {w->Y[3], w->Y[2], w->Y[1], w->Y[0]};
+  if (grad_v) {
+    const int ch = std::max(1, std::min(p->chunk, nst));
+    QBG_TRY(ensure((void**)&w->fields, &w->fields_bytes, sizeof(double2) * 8 * (size_t)ch * p->N));
+    for (int s0 = 0; s0 < nst; s0 += ch) {
+      const int ns = std::min(ch, nst - s0);
+      for (int m = 0; m < 4; ++m) {
+        QBG_TRY(field_bwd(p, M[m] + (size_t)s0 * ld, ld, w->fields + (size_t)m * ns * p->N, ns, st));
+        QBG_TRY(field_bwd(p, xv[m] + (size_t)s0 * ld, ld, w->fields + (size_t)(4 + m) * ns * p->N,
+                          ns, st));
+      }
+      k_grad_v<<<(unsigned)((p->N + 255) / 256), 256, 0, st>>>(w->fields, ns, p->N,
+                                                               2.0 / (double)p->N, grad_v);
+      QBG_LAUNCHED(p);
+    }
+  }
+  if (ga) {
+    Quad q;
+    for (int m = 0; m < 4; ++m) {
+      q.M[m] = M[m];
+      q.X[m] = xv[m];
+    }
+    const int gx = std::min(64, (p->ngw + 255) / 256);
+    const size_t nkin = (size_t)gx * nst;
+    const int P = p->nproj;
+    const size_t total = (size_t)nst * P;
+    const size_t nnl = P ? (total + 255) / 256 : 0;
+    QBG_TRY(ensure((void**)&w->part, &w->part_bytes, sizeof(double) * std::max(nkin, nnl)));
+    k_grad_kin<<<dim3(gx, nst), 256, 0, st>>>(q, ld, p->ngw, p->d_kpgx, p->A[0], p->A[1], p->A[2],
+                                             e[0], e[1], e[2], w->part);
+    QBG_LAUNCHED(p);
+    double skin = 0.0, snl = 0.0;
+    QBG_TRY(sum_part(p, w, nkin, &skin, st));
+    if (P > 0) {
+      QBG_TRY(ensure_dtable(p, w, e, st));
+      QBG_TRY(ensure((void**)&w->proj, &w->proj_bytes, sizeof(double2) * 16 * total));
+      for (int m = 0; m < 4; ++m) {
+        QBG_TRY(project(p, w, false, M[m], ld, nst, w->proj + (size_t)m * total, st));
+        QBG_TRY(project(p, w, false, xv[m], ld, nst, w->proj + (size_t)(4 + m) * total, st));
+        QBG_TRY(project(p, w, true, M[m], ld, nst, w->proj + (size_t)(8 + m) * total, st));
+        QBG_TRY(project(p, w, true, xv[m], ld, nst, w->proj + (size_t)(12 + m) * total, st));
+      }
+      k_grad_nl<<<(unsigned)nnl, 256, 0, st>>>(w->proj, nst, P, p->d_pwt, w->part);
+      QBG_LAUNCHED(p);
+      QBG_TRY(sum_part(p, w, nnl, &snl, st));
+    }
+    *ga += 2.0 * (skin + snl);
+  }
+  return QBG_OK;
+}
+
+static qbg_status set_A(qbg_plan* p, const double* A, cudaStream_t st) {
+  if (A) QBG_TRY(qbg_set_vector_potential(p, A));
+  return ensure_nl(p, st);
+}
+
+static qbg_status direct_term(qbg_plan* p, AdjWork* w, const double2* psi, int ld, int nst,
+                              const double* g, double2* lam, cudaStream_t st) {
+  if (g[0] == 0.0 && g[1] == 0.0 && g[2] == 0.0) return QBG_OK;
+  k_direct<<<dim3((p->ngw + 255) / 256, nst), 256, 0, st>>>(psi, ld, p->ngw, p->d_kpgx, w->occ,
+                                                           g[0], g[1], g[2], lam);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+static qbg_status upload_adj_occ(AdjWork* w, const double* occ, int nst) {
+  QBG_TRY(ensure((void**)&w->occ, &w->occ_bytes, sizeof(double) * std::max(nst, 1)));
+  std::vector<double> h(std::max(nst, 1), 0.0);
+  for (int s = 0; s < nst; ++s) h[s] = occ ? occ[s] : 0.0;
+  QBG_CUDA(cudaMemcpy(w->occ, h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+  return QBG_OK;
+}
+
+// adjoint of one step: lambda <- P_a^+ P_b^+ lambda, gradients accumulated
+static qbg_status adjoint_step(qbg_plan* p, AdjWork* w, const double2* psi_n, const double2* phi_n,
+                               int ld, int nst, const double* d_occ, double dt, const double* A_n,
+                               const double* A_np1, const double* e, double2* lam,
+                               double* grad_v, double* grad_a, cudaStream_t st) {
+  const double tau = 0.5 * dt;
+  if (!phi_n) {
+    QBG_TRY(set_A(p, A_n, st));
+    QBG_TRY(ensure((void**)&w->phi, &w->phi_bytes, sizeof(double2) * (size_t)ld * nst));
+    QBG_CUDA(cudaMemcpyAsync(w->phi, psi_n, sizeof(double2) * (size_t)ld * nst,
+                             cudaMemcpyDeviceToDevice, st));
+    QBG_TRY(exponential(p, w->phi, ld, nst, d_occ, tau, st));
+    phi_n = w->phi;
+  }
+  QBG_TRY(set_A(p, A_np1, st));
+  QBG_TRY(adj_factor(p, w, phi_n, lam, w->chi, ld, nst, d_occ, tau, e, grad_v,
+                     grad_a ? grad_a + 1 : nullptr, st));
+  QBG_TRY(set_A(p, A_n, st));
+  QBG_TRY(adj_factor(p, w, psi_n, w->chi, lam, ld, nst, d_occ, tau, e, grad_v,
+                     grad_a ? grad_a : nullptr, st));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
+  return QBG_OK;
+}
+
+}  // namespace qbg
+
+struct qbg_td {
+  qbg_plan* p = nullptr;
+  int ld = 0, nst = 0, nsteps = 0, K = 0;
+  double dt = 0.0, nel = 0.0;
+  std::vector<double> occ, A;          // A: [(nsteps+1) x 3]
+  std::vector<double2*> ckpt;          // psi_n at n = 0, K, 2K, ...
+  std::vector<double2*> seg_psi, seg_phi;  // psi_n and P_a psi_n of one segment
+  double2* cur = nullptr;              // state being recomputed
+  double2* lam = nullptr;              // adjoint state
+  bool have_forward = false;
+};
+
+namespace qbg {
+
+static void td_free(qbg_td* td) {
+  if (!td) return;
+  for (auto* v : {&td->ckpt, &td->seg_psi, &td->seg_phi})
+    for (double2* b : *v)
+      if (b) cudaFree(b);
+  if (td->cur) cudaFree(td->cur);
+  if (td->lam) cudaFree(td->lam);
+  delete td;
+}
+
+static qbg_status copy_states(const qbg_td* td, const double2* src, double2* dst, cudaStream_t st) {
+  QBG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double2) * (size_t)td->ld * td->nst,
+                           cudaMemcpyDeviceToDevice, st));
+  return QBG_OK;
+}
+
+// one fixed-potential ETRS step of x (the psi result equals that of
+// qbg_etrs_step with the same A_t, A_tdt); optional copies of psi_n and of
+// the half step P_a psi_n
+static qbg_status td_step(qbg_td* td, double2* x, int n, double2* psi_copy, double2* phi_copy,
+                          cudaStream_t st) {
+  qbg_plan* p = td->p;
+  const double tau = 0.5 * td->dt;
+  if (psi_copy) QBG_TRY(copy_states(td, x, psi_copy, st));
+  QBG_TRY(set_A(p, &td->A[3 * (size_t)n], st));
+  QBG_TRY(exponential(p, x, td->ld, td->nst, nullptr, tau, st));
+  if (phi_copy) QBG_TRY(copy_states(td, x, phi_copy, st));
+  QBG_TRY(set_A(p, &td->A[3 * (size_t)(n + 1)], st));
+  QBG_TRY(exponential(p, x, td->ld, td->nst, nullptr, tau, st));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
+  return QBG_OK;
+}
+
+}  // namespace qbg
+
+using namespace qbg;
+
+extern "C" {
+
+qbg_status qbg_etrs_adjoint_step(qbg_plan* p, const double* psi_n, const double* phi_n, int ld,
+                                 int nst, const double* occ, double dt, const double* A_n,
+                                 const double* A_np1, const double* e, double* lambda,
+                                 double* grad_v, double* grad_a, void* stream) {
+  QBG_TRY(check_common(p, psi_n, ld, nst, "qbg_etrs_adjoint_step"));
+  if (nst > 0 && !lambda) {
+    set_error("qbg_etrs_adjoint_step: null lambda");
+    return QBG_ERR_INVALID;
+  }
+  if (grad_a && !e) {
+    set_error("qbg_etrs_adjoint_step: grad_a needs the direction e");
+    return QBG_ERR_INVALID;
+  }
+  if (nst == 0) return QBG_OK;
+  (void)occ;
+  cudaStream_t st = (cudaStream_t)stream;
+  AdjWork* w = work_of(p);
+  QBG_TRY(work_vectors(w, sizeof(double2) * (size_t)ld * nst));
+  return adjoint_step(p, w, (const double2*)psi_n, (const double2*)phi_n, ld, nst, nullptr, dt,
+                      A_n, A_np1, e, (double2*)lambda, grad_v, grad_a, st);
+}
+
+qbg_status qbg_td_create(qbg_plan* p, int ld, int nst, const double* occ, double dt, int nsteps,
+                         int K, qbg_td** out) {
+  if (!out || !p || nst <= 0 || ld < p->ngw || nsteps < 1 || K <= 0 || !occ) {
+    set_error("qbg_td_create: invalid argument");
+    return QBG_ERR_INVALID;
+  }
+  *out = nullptr;
+  qbg_td* td = new qbg_td;
+  td->p = p;
+  td->ld = ld;
+  td->nst = nst;
+  td->nsteps = nsteps;
+  td->K = std::min(K, nsteps);
+  td->dt = dt;
+  td->occ.assign(occ, occ + nst);
+  for (double o : td->occ) td->nel += o;
+  td->A.assign(3 * (size_t)(nsteps + 1), 0.0);
+  const size_t bytes = sizeof(double2) * (size_t)ld * nst;
+  const int nseg = (nsteps + td->K - 1) / td->K;
+  td->ckpt.assign(nseg, nullptr);
+  td->seg_psi.assign(td->K, nullptr);
+  td->seg_phi.assign(td->K, nullptr);
+  std::vector<double2**> all;
+  for (auto& b : td->ckpt) all.push_back(&b);
+  for (auto& b : td->seg_psi) all.push_back(&b);
+  for (auto& b : td->seg_phi) all.push_back(&b);
+  all.push_back(&td->cur);
+  all.push_back(&td->lam);
+  for (double2** b : all) {
+    const cudaError_t e = cudaMalloc((void**)b, bytes);
+    if (e != cudaSuccess) {
+      *b = nullptr;
+      td_free(td);
+      return cuda_status(e, "qbg_td_create");
+    }
+  }
+  *out = td;
+  return QBG_OK;
+}
+
+qbg_status qbg_td_forward(qbg_td* td, double* psi_, const double* A, double* J, void* stream) {
+  if (!td || !psi_ || !A) {
+    set_error("qbg_td_forward: invalid argument");
+    return QBG_ERR_INVALID;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  qbg_plan* p = td->p;
+  double2* psi = (double2*)psi_;
+  td->A.assign(A, A + 3 * (size_t)(td->nsteps + 1));
+  td->have_forward = false;
+  QBG_TRY(set_A(p, &td->A[0], st));
+  if (J) QBG_TRY(qbg_current(p, psi_, td->ld, td->nst, td->occ.data(), td->nel, J, stream));
+  for (int n = 0; n < td->nsteps; ++n) {
+    QBG_TRY(td_step(td, psi, n, n % td->K == 0 ? td->ckpt[n / td->K] : nullptr, nullptr, st));
+    if (J)
+      QBG_TRY(qbg_current(p, psi_, td->ld, td->nst, td->occ.data(), td->nel,
+                          J + 3 * (size_t)(n + 1), stream));
+  }
+  QBG_CUDA(cudaStreamSynchronize(st));
+  td->have_forward = true;
+  return QBG_OK;
+}
+
+qbg_status qbg_td_backward(qbg_td* td, const double* dLdJ, const double* e, double* grad_v,
+                           double* grad_a, double* lambda0, void* stream) {
+  if (!td || !dLdJ || (grad_a && !e)) {
+    set_error("qbg_td_backward: invalid argument");
+    return QBG_ERR_INVALID;
+  }
+  if (!td->have_forward) {
+    set_error("qbg_td_backward: no forward pass recorded");
+    return QBG_ERR_STATE;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  qbg_plan* p = td->p;
+  AdjWork* w = work_of(p);
+  const int nst = td->nst, ld = td->ld, N = td->nsteps, K = td->K;
+  QBG_TRY(work_vectors(w, sizeof(double2) * (size_t)ld * nst));
+  QBG_TRY(upload_adj_occ(w, td->occ.data(), nst));
+  const double zero_e[3] = {0, 0, 0};
+  const double* ev = e ? e : zero_e;
+  if (grad_v) QBG_CUDA(cudaMemsetAsync(grad_v, 0, sizeof(double) * p->N, st));
+  if (grad_a)
+    for (int n = 0; n <= N; ++n) grad_a[n] = 0.0;
+  // explicit A dependence of J_n: dJ_d/da_n = nel e_d
+  auto explicit_a = [&](int n) {
+    if (grad_a)
+      grad_a[n] += td->nel * (dLdJ[3 * n] * ev[0] + dLdJ[3 * n + 1] * ev[1] + dLdJ[3 * n + 2] * ev[2]);
+  };
+  QBG_CUDA(cudaMemsetAsync(td->lam, 0, sizeof(double2) * (size_t)ld * nst, st));
+  const int nseg = (N + K - 1) / K;
+  for (int seg = nseg - 1; seg >= 0; --seg) {
+    const int s0 = seg * K, s1 = std::min(N, s0 + K);
+    // recompute the segment from its checkpoint
+    QBG_TRY(copy_states(td, td->ckpt[seg], td->cur, st));
+    for (int n = s0; n < s1; ++n)
+      QBG_TRY(td_step(td, td->cur, n, td->seg_psi[n - s0], td->seg_phi[n - s0], st));
+    if (seg == nseg - 1) {  // cur = psi_N
+      QBG_TRY(direct_term(p, w, td->cur, ld, nst, dLdJ + 3 * (size_t)N, td->lam, st));
+      explicit_a(N);
+    }
+    for (int n = s1 - 1; n >= s0; --n) {
+      QBG_TRY(adjoint_step(p, w, td->seg_psi[n - s0], td->seg_phi[n - s0], ld, nst, nullptr,
+                           td->dt, &td->A[3 * (size_t)n], &td->A[3 * (size_t)(n + 1)],
+                           ev, td->lam, grad_v, grad_a ? grad_a + n : nullptr, st));
+      QBG_TRY(direct_term(p, w, td->seg_psi[n - s0], ld, nst, dLdJ + 3 * (size_t)n, td->lam, st));
+      explicit_a(n);
+    }
+  }
+  if (lambda0) QBG_TRY(copy_states(td, td->lam, (double2*)lambda0, st));
+  QBG_CUDA(cudaStreamSynchronize(st));
+  return QBG_OK;
+}
+
+qbg_status qbg_td_destroy(qbg_td* td) {
+  td_free(td);
+  return QBG_OK;
+}
+
+}  // extern "C"

@@ -1275,6 +1275,8 @@ template qbg_status local_hpsi<double>(qbg_plan*, const double2*, int, double2*,
 template qbg_status local_hpsi<float>(qbg_plan*, const double2*, int, double2*, int, bool,
                                       double2*, int, double2, cudaStream_t);
 template qbg_status backward<double>(qbg_plan*, const double2*, int, double2*, int, cudaStream_t);
+template qbg_status backward<float>(qbg_plan*, const double2*, int, double2*, int, cudaStream_t);
+template qbg_status backward<df32>(qbg_plan*, const double2*, int, double2*, int, cudaStream_t);
 template qbg_status forward<double>(qbg_plan*, double2*, double2*, int, int, cudaStream_t);
 template qbg_status density<double>(qbg_plan*, const double2*, int, int, const double*, double*,
                                     cudaStream_t);

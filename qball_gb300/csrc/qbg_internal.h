@@ -110,7 +110,6 @@ struct qbg_plan {
   bool check_every_step = true; // read the tensor-core status word after each step
   bool lane_fft = true;         // register-resident lane-group transforms where supported
   bool fuse_xyx = true;         // x, y and x passes of H psi in one kernel where they fit
-  int tc_nst_cleared = 0;
 
   // scratch (allocated lazily, grown as needed)
   void* d_Z = nullptr;  size_t Z_bytes = 0;   // [chunk][n2][nrods]
@@ -140,6 +139,7 @@ struct qbg_plan {
   double* d_hxc_red = nullptr;   // energy partials [3][kHxcBlocks]
   bool have_ionic = false;
   bool selfconsistent = false;
+  void* adj = nullptr;           // adjoint work buffers (qbg_adjoint.cu)
 };
 
 namespace qbg {
@@ -216,6 +216,28 @@ qbg_status tc_check_status(qbg_plan* p);
 
 // misc kernels (qbg_ops.cu)
 qbg_status update_kinetic(qbg_plan* p, cudaStream_t st);
+// operator helpers (qbg_ops.cu)
+qbg_status upload_occ(qbg_plan* p, const double* occ, int nst, double scale, double** d_out,
+                      cudaStream_t st);
+qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
+                     const double* d_occ, double* enl_part, int* enl_blocks, double2* acc,
+                     int ldacc, double2 fac, cudaStream_t st);
+bool uses_tc(const qbg_plan* p);
+qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, const char* who);
+qbg_status ensure_nl(qbg_plan* p, cudaStream_t st);
+// psi <- sum_{k<=4} (-i dt1 H)^k / k! psi (FP64 accumulation)
+qbg_status exponential(qbg_plan* p, double2* psi, int ld, int nst, const double* d_occ,
+                       double dt1, cudaStream_t st);
+
+// adjoint support (qbg_nl.cu, qbg_tc.cu)
+qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_t st);
+qbg_status nl_project64(qbg_plan* p, const double2* table, const double2* x, int ld, int nst,
+                        double2* f, cudaStream_t st);
+qbg_status tc_proj_build(qbg_plan* p, const double2* table, void** out, cudaStream_t st);
+void tc_proj_free(void* proj);
+qbg_status tc_project(qbg_plan* p, const void* proj, const double2* x, int ld, int nst,
+                      double2* f, cudaStream_t st);
+void adj_release(qbg_plan* p);
 
 // Hartree + xc (qbg_hxc.cu): v_r from rho (device), energies stay on the
 // device until read

@@ -108,12 +108,10 @@ qbg_status update_kinetic(qbg_plan* p, cudaStream_t st) {
   return QBG_OK;
 }
 
-qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
-  // projector order: species, atom blocks of <= 128 atoms, projector ipr
-  // (l, then m), atom within the block -- the index ia + ipr*nblk of
-  // NonLocalPotential.cc:2000 taken block by block.
-  std::vector<ProjDesc> pd;
-  std::vector<double> wt;
+// projector order: species, atom blocks of <= 128 atoms, projector ipr
+// (l, then m), atom within the block -- the index ia + ipr*nblk of
+// NonLocalPotential.cc:2000 taken block by block.
+static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector<double>& wt) {
   int namax = 0;
   for (int s = 0; s < p->nsp; ++s) namax = std::max(namax, p->sp_na[s]);
   const int nbs = std::max(1, std::min(namax, 128));
@@ -137,6 +135,12 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
     }
     atom0 += na;
   }
+}
+
+qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
+  std::vector<ProjDesc> pd;
+  std::vector<double> wt;
+  proj_descs(p, pd, wt);
   p->nproj = (int)pd.size();
   tc_release(p);
   if (p->d_ptau) cudaFree(p->d_ptau);
@@ -381,5 +385,119 @@ int nl_reduce_blocks(const qbg_plan* p, int nst) {
 
 template qbg_status nl_apply<double>(qbg_plan*, const double2*, int, double2*, int,
                                      const double*, double*, cudaStream_t);
+
+// ------------------------------------------------- derivative of the table
+// dbeta[p][g] = d anl[p][g] / da for A = A0 + a e: the projector k_anl builds
+// is kappa_l t(q) exp(-i q.tau) with q = k+G-A, kappa = 1, -i, -1 for
+// l = 0, 1, 2 and t = s_l P_lm(q) exp(-|q|^2 rc^2 / 2) (P_lm the solid
+// harmonic: 1, q_m, the five quadratics), so with dq/da = -e
+//   dbeta = -kappa exp(-i q.tau) (e.grad t - i (e.tau) t),
+//   e.grad t = s_l (e.grad P - rc^2 P (e.q)) exp(-|q|^2 rc^2 / 2).
+__global__ void k_anl_da(const double* __restrict__ kpgx, const double* __restrict__ kpg2A,
+                         int ngw, double A0, double A1, double A2, double e0, double e1,
+                         double e2, const ProjDesc* __restrict__ pd, int nproj,
+                         double2* __restrict__ dbeta) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int p = blockIdx.y;
+  if (g >= ngw || p >= nproj) return;
+  const ProjDesc d = pd[p];
+  const double qx = kpgx[g] - A0, qy = kpgx[ngw + g] - A1, qz = kpgx[2 * ngw + g] - A2;
+  const double rc2 = d.rc * d.rc;
+  const double E = exp(-0.5 * kpg2A[g] * rc2);
+  const double eq = e0 * qx + e1 * qy + e2 * qz;
+  const double fpi = 4.0 * 3.14159265358979323846;
+  double P, eP, s;
+  if (d.l == 0) {
+    s = sqrt(1.0 / fpi);
+    P = 1.0;
+    eP = 0.0;
+  } else if (d.l == 1) {
+    s = sqrt(3.0 / fpi);
+    P = d.m == 0 ? qx : (d.m == 1 ? qy : qz);
+    eP = d.m == 0 ? e0 : (d.m == 1 ? e1 : e2);
+  } else {
+    const double s3 = sqrt(3.0);
+    s = sqrt(5.0 / fpi);
+    switch (d.m) {
+      case 0: P = 0.5 * (2.0 * qz * qz - qx * qx - qy * qy);
+              eP = -e0 * qx - e1 * qy + 2.0 * e2 * qz; break;
+      case 1: P = 0.5 * s3 * (qx * qx - qy * qy); eP = s3 * (e0 * qx - e1 * qy); break;
+      case 2: P = s3 * qx * qy; eP = s3 * (e0 * qy + e1 * qx); break;
+      case 3: P = s3 * qy * qz; eP = s3 * (e1 * qz + e2 * qy); break;
+      default: P = s3 * qx * qz; eP = s3 * (e0 * qz + e2 * qx); break;
+    }
+  }
+  const double t = s * P * E;
+  const double wr = s * E * (eP - rc2 * P * eq);
+  const double wi = -(e0 * d.tau[0] + e1 * d.tau[1] + e2 * d.tau[2]) * t;
+  double sn, cs;
+  sincos(-(d.tau[0] * qx + d.tau[1] * qy + d.tau[2] * qz), &sn, &cs);
+  const double zr = cs * wr - sn * wi, zi = sn * wr + cs * wi;
+  double2 o;
+  if (d.l == 0) o = make_double2(-zr, -zi);
+  else if (d.l == 1) o = make_double2(-zi, zr);
+  else o = make_double2(zr, zi);
+  dbeta[(size_t)p * ngw + g] = o;
+}
+
+qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_t st) {
+  std::vector<ProjDesc> pd;
+  std::vector<double> wt;
+  proj_descs(p, pd, wt);
+  if ((int)pd.size() != p->nproj) {
+    set_error("projector derivative: the projector list changed");
+    return QBG_ERR_STATE;
+  }
+  if (pd.empty() || p->ngw == 0) return QBG_OK;
+  ProjDesc* d_pd = nullptr;
+  QBG_CUDA(cudaMalloc(&d_pd, sizeof(ProjDesc) * pd.size()));
+  QBG_CUDA(cudaMemcpy(d_pd, pd.data(), sizeof(ProjDesc) * pd.size(), cudaMemcpyHostToDevice));
+  dim3 grid((p->ngw + 255) / 256, p->nproj);
+  k_anl_da<<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2], e[0],
+                                 e[1], e[2], d_pd, p->nproj, dbeta);
+  p->launches++;
+  cudaError_t err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+  cudaFree(d_pd);
+  if (err != cudaSuccess) return cuda_status(err, "k_anl_da");
+  return QBG_OK;
+}
+
+// f[n][p] = sum_z part[z][n][p]
+__global__ void k_part_sum(const double2* __restrict__ part, int nsplit, size_t total,
+                           double2* __restrict__ f) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  double re = 0.0, im = 0.0;
+  for (int z = 0; z < nsplit; ++z) {
+    const double2 v = part[(size_t)z * total + i];
+    re += v.x;
+    im += v.y;
+  }
+  f[i] = make_double2(re, im);
+}
+
+// f[n][p] = sum_g conj(table[p][g]) x[n][g] in FP64 (no weights)
+qbg_status nl_project64(qbg_plan* p, const double2* table, const double2* x, int ld, int nst,
+                        double2* f, cudaStream_t st) {
+  const int P = p->nproj;
+  if (P == 0 || nst == 0) return QBG_OK;
+  const int mt = (P + GT - 1) / GT, nt = (nst + GT - 1) / GT;
+  int split = std::max(1, (4 * 152 + mt * nt - 1) / (mt * nt));
+  split = std::min(split, std::max(1, p->ngw / GK));
+  int kchunk = (p->ngw + split - 1) / split;
+  kchunk = (kchunk + GK - 1) / GK * GK;
+  split = (p->ngw + kchunk - 1) / kchunk;
+  const qbg_status s = ensure(&p->d_fpart, &p->fpart_bytes, (size_t)split * P * nst * sizeof(double2));
+  if (s != QBG_OK) return s;
+  k_fnl<double><<<dim3(mt, nt, split), 256, 0, st>>>(table, p->ngw, P, x, ld, nst,
+                                                      (double2*)p->d_fpart, kchunk);
+  QBG_LAUNCHED(p);
+  const size_t total = (size_t)P * nst;
+  k_part_sum<<<(unsigned)((total + 255) / 256), 256, 0, st>>>((const double2*)p->d_fpart, split,
+                                                              total, f);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
 
 }  // namespace qbg

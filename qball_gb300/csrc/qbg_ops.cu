@@ -88,7 +88,7 @@ __global__ void k_current(const double2* __restrict__ c, int ld, int ngw,
   }
 }
 
-static qbg_status upload_occ(qbg_plan* p, const double* occ, int nst, double scale,
+qbg_status upload_occ(qbg_plan* p, const double* occ, int nst, double scale,
                              double** d_out, cudaStream_t st) {
   // the reduction buffer's tail holds per-state factors
   static_assert(sizeof(double) == 8, "");
@@ -112,7 +112,7 @@ static qbg_status upload_occ(qbg_plan* p, const double* occ, int nst, double sca
 // transforms and projector GEMMs in FP64; the mixed form runs the transforms
 // in FP32 and the projector GEMMs on the tensor cores.  When acc is set,
 // acc += fac * (H psi) is fused into the last pass.
-static qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
+qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
                             const double* d_occ, double* enl_part, int* enl_blocks,
                             double2* acc, int ldacc, double2 fac, cudaStream_t st) {
   const bool nl = p->nproj > 0;
@@ -139,12 +139,12 @@ static qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* ou
   return local_hpsi<float>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
 }
 
-static bool uses_tc(const qbg_plan* p) {
+bool uses_tc(const qbg_plan* p) {
   return p->prec == QBG_PREC_MIXED || p->prec == QBG_PREC_MIXED_FFT64 ||
          p->prec == QBG_PREC_MIXED_DF32;
 }
 
-static qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, const char* who) {
+qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, const char* who) {
   if (!p || nst < 0 || ld < p->ngw || (nst > 0 && !a)) {
     set_error("%s: invalid argument (ld=%d, ngw=%d, nst=%d)", who, ld, p ? p->ngw : -1, nst);
     return QBG_ERR_INVALID;
@@ -152,8 +152,32 @@ static qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, cons
   return QBG_OK;
 }
 
-static qbg_status ensure_nl(qbg_plan* p, cudaStream_t st) {
+qbg_status ensure_nl(qbg_plan* p, cudaStream_t st) {
   if (p->nsp > 0 && !p->nl_ready) return nl_build(p, st);
+  return QBG_OK;
+}
+
+// exponential(1, dt1) of ExponentialWavefunctionStepper.cc:51-148: the
+// Taylor series is accumulated straight into psi (FP64); the four H
+// applications ping-pong between two FP64 work buffers.
+qbg_status exponential(qbg_plan* p, double2* psi, int ld, int nst, const double* d_occ,
+                              double dt1, cudaStream_t st) {
+  double f_re = 1.0, f_im = 0.0;
+  const size_t n64 = sizeof(double2) * (size_t)ld * nst;
+  QBG_TRY(ensure(&p->d_w[0], &p->w_bytes[0], n64));
+  QBG_TRY(ensure(&p->d_w[1], &p->w_bytes[1], n64));
+  for (int N = 1; N <= 4; ++N) {
+    // factor1 *= -complex(0,1)*dt1/double(N)
+    const double m_re = -0.0 * dt1 / (double)N, m_im = -1.0 * dt1 / (double)N;
+    const double n_re = f_re * m_re - f_im * m_im, n_im = f_re * m_im + f_im * m_re;
+    f_re = n_re;
+    f_im = n_im;
+    const double2 fac = make_double2(f_re, f_im);
+    const double2* in = N == 1 ? psi : (const double2*)p->d_w[N & 1];
+    double2* out = (double2*)p->d_w[(N - 1) & 1];
+    int nb;
+    QBG_TRY(hpsi_core(p, in, ld, out, nst, d_occ, nullptr, &nb, psi, ld, fac, st));
+  }
   return QBG_OK;
 }
 
@@ -368,30 +392,6 @@ qbg_status qbg_current(qbg_plan* p, const double* psi, int ld, int nst, const do
       for (int d = 0; d < 3; ++d) s[d] += p->h_red[3 * b + d];
   }
   for (int d = 0; d < 3; ++d) J[d] = -s[d] + p->A[d] * nel;
-  return QBG_OK;
-}
-
-// exponential(1, dt1) of ExponentialWavefunctionStepper.cc:51-148: the
-// Taylor series is accumulated straight into psi (FP64); the four H
-// applications ping-pong between two FP64 work buffers.
-static qbg_status exponential(qbg_plan* p, double2* psi, int ld, int nst, const double* d_occ,
-                              double dt1, cudaStream_t st) {
-  double f_re = 1.0, f_im = 0.0;
-  const size_t n64 = sizeof(double2) * (size_t)ld * nst;
-  QBG_TRY(ensure(&p->d_w[0], &p->w_bytes[0], n64));
-  QBG_TRY(ensure(&p->d_w[1], &p->w_bytes[1], n64));
-  for (int N = 1; N <= 4; ++N) {
-    // factor1 *= -complex(0,1)*dt1/double(N)
-    const double m_re = -0.0 * dt1 / (double)N, m_im = -1.0 * dt1 / (double)N;
-    const double n_re = f_re * m_re - f_im * m_im, n_im = f_re * m_im + f_im * m_re;
-    f_re = n_re;
-    f_im = n_im;
-    const double2 fac = make_double2(f_re, f_im);
-    const double2* in = N == 1 ? psi : (const double2*)p->d_w[N & 1];
-    double2* out = (double2*)p->d_w[(N - 1) & 1];
-    int nb;
-    QBG_TRY(hpsi_core(p, in, ld, out, nst, d_occ, nullptr, &nb, psi, ld, fac, st));
-  }
   return QBG_OK;
 }
 

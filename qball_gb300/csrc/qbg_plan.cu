@@ -468,6 +468,7 @@ qbg_status qbg_basis_fill(const double* a, double ecut, int* rod_h, int* rod_k,
 
 qbg_status qbg_plan_destroy(qbg_plan* p) {
   if (!p) return QBG_OK;
+  adj_release(p);
   tc_release(p);
   hxc_release(p);
   for (auto& L : p->len) free_len(L);

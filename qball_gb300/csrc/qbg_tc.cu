@@ -583,7 +583,6 @@ static void tc_free(TcTables* t) {
 void tc_release(qbg_plan* p) {
   tc_free((TcTables*)p->tc);
   p->tc = nullptr;
-  p->tc_nst_cleared = 0;
 }
 
 qbg_status tc_build(qbg_plan* p, cudaStream_t st) {
@@ -644,41 +643,35 @@ static qbg_status tc_launch(qbg_plan* p, int mode, const TcArgs& a, int mt, int 
   return QBG_OK;
 }
 
-// out[n][g] = sum_p anl[p][g] fnl[n][p] with fnl = D/Omega <anl|psi>; psi and
-// out are FP64 [ld x nst]; enl partial sums into enl_part when given.
-qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
-                       const double* d_occ, double* enl_part, int* enl_blocks,
-                       cudaStream_t st) {
-  TcTables* t = (TcTables*)p->tc;
-  if (!t) QBG_TRY_TC(tc_build(p, st));
-  t = (TcTables*)p->tc;
-  if (!t) return QBG_OK;
+// Grows a piece array; a new allocation is cleared (its padding rows must
+// stay zero).
+static qbg_status ensure_pieces(__half** buf, size_t* cur, size_t need, cudaStream_t st) {
+  const void* before = *buf;
+  QBG_TRY_TC(ensure((void**)buf, cur, need));
+  if (*buf != before) QBG_CUDA(cudaMemsetAsync(*buf, 0, *cur, st));
+  return QBG_OK;
+}
+
+// GEMM1 of a projector table X1 (scales s1; x1_RT x x1_KS pieces of the
+// plan's layout) with the nst vectors x: split x into t->Y, leave the split-K
+// partial sums in t->part ([nsplit][nst][2P]) and return nsplit.
+static qbg_status tc_gemm1(qbg_plan* p, TcTables* t, const __half* X1, const float* s1,
+                           const double2* x, int ld, int nst, int* nsplit_out, cudaStream_t st) {
   const int P = t->P, ngw = t->ngw;
   const int nRT = (nst + TC_N - 1) / TC_N;
-  // split psi
-  QBG_TRY_TC(ensure((void**)&t->Y, &t->Y_bytes, pieces_bytes(nRT, t->x1_KS)));
+  QBG_TRY_TC(ensure_pieces(&t->Y, &t->Y_bytes, pieces_bytes(nRT, t->x1_KS), st));
   QBG_TRY_TC(ensure((void**)&t->sY, &t->sY_bytes, sizeof(float) * nRT * TC_N));
   QBG_TRY_TC(ensure((void**)&t->rmax, &t->rmax_bytes, sizeof(double) * nRT * TC_N));
-  QBG_TRY_TC(ensure((void**)&t->F, &t->F_bytes, pieces_bytes(nRT, t->x2_KS)));
-  QBG_TRY_TC(ensure((void**)&t->sF, &t->sF_bytes, sizeof(float) * nRT * TC_N));
-  QBG_TRY_TC(ensure((void**)&t->fnl, &t->fnl_bytes, sizeof(double2) * (size_t)P * nst));
-  // the padding rows of the piece arrays stay zero: clear once per growth
-  if (t->Y_bytes && p->tc_nst_cleared < nst) {
-    QBG_CUDA(cudaMemsetAsync(t->Y, 0, t->Y_bytes, st));
-    QBG_CUDA(cudaMemsetAsync(t->F, 0, t->F_bytes, st));
-    p->tc_nst_cleared = nst;
-  }
   {
     PhaseTimer pt(p, PH_MISC, st);
     QBG_CUDA(cudaMemsetAsync(t->rmax, 0, sizeof(double) * nst, st));
-    k_rowmax_c64<<<dim3(std::min(32, (ngw + 255) / 256), nst), 256, 0, st>>>(psi, ld, ngw,
+    k_rowmax_c64<<<dim3(std::min(32, (ngw + 255) / 256), nst), 256, 0, st>>>(x, ld, ngw,
                                                                            t->rmax);
     QBG_LAUNCHED(p);
-    k_split_rows4<<<dim3((ngw + 1023) / 1024, nst), 256, 0, st>>>(psi, ld, ngw, t->rmax, t->Y,
+    k_split_rows4<<<dim3((ngw + 1023) / 1024, nst), 256, 0, st>>>(x, ld, ngw, t->rmax, t->Y,
                                                                  nRT, t->x1_KS, t->sY);
     QBG_LAUNCHED(p);
   }
-  // GEMM1 with split K
   const int mt1 = t->x1_RT;
   // split K so that the CTAs (one per SM) fill their last wave: the time is
   // ~ waves / nsplit, waves = ceil(tiles * nsplit / SMs); at least ~3 waves
@@ -704,7 +697,7 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
   nsplit = (t->x1_KS + ksp - 1) / ksp;
   QBG_TRY_TC(ensure((void**)&t->part, &t->part_bytes, sizeof(double) * nsplit * nst * 2 * P));
   TcArgs a1;
-  a1.A = t->X1;
+  a1.A = X1;
   a1.B = t->Y;
   a1.nRTa = t->x1_RT;
   a1.nRTb = nRT;
@@ -712,7 +705,7 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
   a1.M = 2 * P;
   a1.N = nst;
   a1.ks_per_split = ksp;
-  a1.sA = t->s1;
+  a1.sA = s1;
   a1.sB = t->sY;
   a1.out = t->part;
   a1.ldo = 0;
@@ -721,6 +714,26 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
     PhaseTimer pt(p, PH_FNL_GEMM, st);
     QBG_TRY_TC(tc_launch(p, TC_OUT_PARTIAL, a1, mt1, nRT, nsplit, st));
   }
+  *nsplit_out = nsplit;
+  return QBG_OK;
+}
+
+// out[n][g] = sum_p anl[p][g] fnl[n][p] with fnl = D/Omega <anl|psi>; psi and
+// out are FP64 [ld x nst]; enl partial sums into enl_part when given.
+qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
+                       const double* d_occ, double* enl_part, int* enl_blocks,
+                       cudaStream_t st) {
+  TcTables* t = (TcTables*)p->tc;
+  if (!t) QBG_TRY_TC(tc_build(p, st));
+  t = (TcTables*)p->tc;
+  if (!t) return QBG_OK;
+  const int P = t->P, ngw = t->ngw;
+  const int nRT = (nst + TC_N - 1) / TC_N;
+  QBG_TRY_TC(ensure_pieces(&t->F, &t->F_bytes, pieces_bytes(nRT, t->x2_KS), st));
+  QBG_TRY_TC(ensure((void**)&t->sF, &t->sF_bytes, sizeof(float) * nRT * TC_N));
+  QBG_TRY_TC(ensure((void**)&t->fnl, &t->fnl_bytes, sizeof(double2) * (size_t)P * nst));
+  int nsplit = 1;
+  QBG_TRY_TC(tc_gemm1(p, t, t->X1, t->s1, psi, ld, nst, &nsplit, st));
   const size_t total = (size_t)P * nst;
   const int rb = (int)((total + 255) / 256);
   *enl_blocks = rb;
@@ -756,6 +769,84 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
     PhaseTimer pt(p, PH_ENL_HPSI, st);
     QBG_TRY_TC(tc_launch(p, TC_OUT_HPSI, a2, t->x2_RT, nRT, 1, st));
   }
+  return QBG_OK;
+}
+
+// ------------------------------------------- projections on other tables
+// A second projector table (the derivative tables of the adjoint) in the
+// same FP16 piece layout as the plan's GEMM1 operand.
+struct TcProj {
+  __half* X1 = nullptr;
+  float* s1 = nullptr;
+};
+
+// f[n][p] = sum_z (part[z][n][2p], part[z][n][2p+1])
+__global__ void k_tc_proj_sum(const double* __restrict__ part, int nsplit, int P, int nst,
+                              double2* __restrict__ f) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (size_t)P * nst) return;
+  const int n = (int)(i / P), q = (int)(i - (size_t)n * P);
+  double re = 0.0, im = 0.0;
+  for (int z = 0; z < nsplit; ++z) {
+    const double* pz = part + ((size_t)z * nst + n) * 2 * P;
+    re += pz[2 * q];
+    im += pz[2 * q + 1];
+  }
+  f[i] = make_double2(re, im);
+}
+
+void tc_proj_free(void* h) {
+  TcProj* q = (TcProj*)h;
+  if (!q) return;
+  if (q->X1) cudaFree(q->X1);
+  if (q->s1) cudaFree(q->s1);
+  delete q;
+}
+
+qbg_status tc_proj_build(qbg_plan* p, const double2* table, void** out, cudaStream_t st) {
+  *out = nullptr;
+  TcTables* t = (TcTables*)p->tc;
+  if (!t) QBG_TRY_TC(tc_build(p, st));
+  t = (TcTables*)p->tc;
+  if (!t) return QBG_OK;
+  TcProj* q = new TcProj;
+  const size_t b1 = pieces_bytes(t->x1_RT, t->x1_KS);
+  double* pmax = nullptr;
+  cudaError_t e = cudaMalloc(&q->X1, b1);
+  if (e == cudaSuccess) e = cudaMalloc(&q->s1, sizeof(float) * 2 * t->P);
+  if (e == cudaSuccess) e = cudaMalloc(&pmax, sizeof(double) * t->P);
+  if (e == cudaSuccess) e = cudaMemsetAsync(q->X1, 0, b1, st);
+  if (e == cudaSuccess) {
+    k_anl_rowmax<<<t->P, 256, 0, st>>>(table, t->P, t->ngw, pmax);
+    dim3 g((t->ngw + 255) / 256, t->P);
+    k_split_x1<<<g, 256, 0, st>>>(table, t->P, t->ngw, pmax, q->X1, t->x1_RT, t->x1_KS, q->s1);
+    p->launches += 2;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (pmax) cudaFree(pmax);
+  if (e != cudaSuccess) {
+    tc_proj_free(q);
+    return cuda_status(e, "tc_proj_build");
+  }
+  *out = q;
+  return QBG_OK;
+}
+
+// f[n][p] = sum_g conj(table[p][g]) x[n][g] on the tensor cores (no
+// weights); proj == nullptr projects on the plan's own table.
+qbg_status tc_project(qbg_plan* p, const void* proj, const double2* x, int ld, int nst,
+                      double2* f, cudaStream_t st) {
+  TcTables* t = (TcTables*)p->tc;
+  if (!t) QBG_TRY_TC(tc_build(p, st));
+  t = (TcTables*)p->tc;
+  if (!t || nst == 0) return QBG_OK;
+  const TcProj* q = (const TcProj*)proj;
+  int nsplit = 1;
+  QBG_TRY_TC(tc_gemm1(p, t, q ? q->X1 : t->X1, q ? q->s1 : t->s1, x, ld, nst, &nsplit, st));
+  const size_t total = (size_t)t->P * nst;
+  k_tc_proj_sum<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(t->part, nsplit, t->P, nst, f);
+  QBG_LAUNCHED(p);
   return QBG_OK;
 }
 
