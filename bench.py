@@ -194,7 +194,8 @@ def enable_hxc(H, cell, p, occ):
 
 
 def make_psi(cell, basis):
-    """Seeded random states, Gram-orthonormalised in FP64 on the device."""
+    """Seeded random states, Gram-orthonormalised in FP64 (the nst x nst
+    factor on the host, the products on the device)."""
     import torch
     rng = np.random.default_rng(cell.seed + 7)
     n, ngw = cell.nst, basis.ngw
@@ -204,10 +205,11 @@ def make_psi(cell, basis):
         s1 = min(n, s0 + 64)
         blk = rng.standard_normal((s1 - s0, ngw)) + 1j * rng.standard_normal((s1 - s0, ngw))
         c[s0:s1] = torch.from_numpy(blk).cuda() * env
-    S = c.conj() @ c.T
-    L = torch.linalg.cholesky(S)
-    out = torch.linalg.solve_triangular(L.conj(), c, upper=False)
-    return out
+    # Gram factor on the host (nst x nst): c <- conj(L)^-1 c with S = L L^H
+    S = (c.conj() @ c.T).cpu().numpy()
+    L = np.linalg.cholesky(S)
+    Linv = np.linalg.inv(np.conj(L))
+    return torch.from_numpy(Linv).cuda() @ c
 
 
 def time_etrs(H, p, occ, dt, A, steps, warmup, stream):

@@ -255,15 +255,14 @@ qbg_status qbg_etrs_step(qbg_plan* plan, double* psi, int ld, int nst,
  *     derivatives along the unit direction e (host double[3]) of the vector
  *     potential, through the kinetic term |k+G-A|^2/2 and the projectors
  *     beta(k+G-A) (NonLocalPotential.cc:1962-2037).
- * psi_n: device state at t_n; phi_n: device half step P(H(A_n)) psi_n or
- * NULL (then recomputed, four more H applications).  A_n, A_np1: host
- * double[3] or NULL (keep the plan's A); the plan is left at A_n.  occ is
- * not used (reserved).  Costs 14 H applications, 16 backward transforms and,
- * with grad_a, 32 projections on the projector tables and their derivative
- * along e.  Synchronises when grad_a is given. */
-qbg_status qbg_etrs_adjoint_step(qbg_plan* plan, const double* psi_n,
-                                 const double* phi_n, int ld, int nst,
-                                 const double* occ, double dt,
+ * psi_n: device state at t_n (not modified).  A_n, A_np1: host double[3] or
+ * NULL (keep the plan's A); the plan is left at A_n.  occ is not used
+ * (reserved).  Runs the forward of the step again (8 H applications,
+ * keeping the Taylor powers and their projections), then 8 H applications,
+ * 16 backward transforms and, with grad_a, 16 projections on the derivative
+ * of the projector table along e.  Synchronises when grad_a is given. */
+qbg_status qbg_etrs_adjoint_step(qbg_plan* plan, const double* psi_n, int ld,
+                                 int nst, const double* occ, double dt,
                                  const double* A_n, const double* A_np1,
                                  const double* e, double* lambda,
                                  double* grad_v, double* grad_a, void* stream);
@@ -272,9 +271,10 @@ qbg_status qbg_etrs_adjoint_step(qbg_plan* plan, const double* psi_n,
  * ETRS steps (nsteps >= 1) with a per-step vector potential (laser field in
  * the velocity gauge, VectorPotential.h:150-160).  The forward pass keeps
  * psi every K steps in device memory (ceil(nsteps/K) copies); the backward
- * pass recomputes each segment of K steps from its checkpoint (keeping
- * psi_n and the half steps of that segment, 2K copies) and runs the adjoint
- * steps in reverse. */
+ * pass recomputes each segment of K steps from its checkpoint, keeping per
+ * step psi_n, the half step, the Taylor powers H^1..3 of both and their
+ * projections (8 state-sized buffers per step, 8K in all), and runs the
+ * adjoint steps in reverse: 16 H applications per step in all. */
 typedef struct qbg_td qbg_td;
 qbg_status qbg_td_create(qbg_plan* plan, int ld, int nst, const double* occ,
                          double dt, int nsteps, int K, qbg_td** td);

@@ -68,7 +68,7 @@ ABI = {
     "qbg_update_vhxc": [_P, _P, _P, _P],
     "qbg_set_selfconsistent": [_P, _I],
     "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
-    "qbg_etrs_adjoint_step": [_P, _P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P],
+    "qbg_etrs_adjoint_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P],
     "qbg_td_create": [_P, _I, _I, _P, _D, _I, _I, _P],
     "qbg_td_forward": [_P, _P, _P, _P, _P],
     "qbg_td_backward": [_P, _P, _P, _P, _P, _P, _P],
@@ -362,7 +362,7 @@ class Hamiltonian(FourierTransform):
         return nel.value if want_nel else None
 
     def etrs_adjoint_step(self, psi_n, lam, dt, A_n=None, A_np1=None, e=None, grad_v=None,
-                          want_grad_a=False, phi_n=None, stream=None):
+                          want_grad_a=False, stream=None):
         """lam <- (adjoint of one fixed-potential ETRS step) lam; grad_v
         (device, N doubles) accumulates dL/dv(r); returns [dL/da_n,
         dL/da_{n+1}] along e when want_grad_a."""
@@ -371,7 +371,7 @@ class Hamiltonian(FourierTransform):
         anp = np.ascontiguousarray(A_np1, np.float64) if A_np1 is not None else None
         ev = np.ascontiguousarray(e, np.float64) if e is not None else None
         ga = np.zeros(2) if want_grad_a else None
-        _check(lib().qbg_etrs_adjoint_step(self.h, _dev_ptr(psi_n), _dev_ptr(phi_n), ldv, n, None,
+        _check(lib().qbg_etrs_adjoint_step(self.h, _dev_ptr(psi_n), ldv, n, None,
                                            float(dt), _np_ptr(an), _np_ptr(anp), _np_ptr(ev),
                                            _dev_ptr(lam), _dev_ptr(grad_v), _np_ptr(ga),
                                            _stream_ptr(stream)), "qbg_etrs_adjoint_step")

@@ -17,8 +17,15 @@
 // For the vector potential along e (A = A0 + a e), the kinetic term gives
 // dH/da = -(k+G-A).e and the projectors V = sum_p |b_p> D_p/Omega <b_p| give
 //   <M|dV/da|X> = sum_p D_p/Omega (conj(<b'_p|M>) <b_p|X> + conj(<b_p|M>) <b'_p|X>)
-// with b' = db/da from k_anl_da.  Each factor costs 7 H applications
-// (H^1..3 x0, H^1..4 y0), 8 backward transforms and 16 projections.
+// with b' = db/da from k_anl_da.
+//
+// The forward of a step (recomputed from a checkpoint) keeps what its
+// adjoint needs: psi_n, the half step P_a psi_n, the powers H^1..3 of both
+// and the weighted projections (D/Omega)<b|H^m x0>, m = 0..3, that its H
+// applications form anyway.  The adjoint of a factor then applies H four
+// times to y0 (keeping the projections of H^0..3 y0) and transforms the
+// eight vectors M_m, H^m x0 to real space: with the recompute, 16 H
+// applications per step against 8 for the forward.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -34,30 +41,63 @@ namespace qbg {
     if (s_ != QBG_OK) return s_;  \
   } while (0)
 
+// What the forward of one step keeps for its adjoint (device buffers).
+struct StepKeep {
+  double2* psi = nullptr;        // psi_n
+  double2* phi = nullptr;        // P_a psi_n
+  double2* pw[2][3] = {};        // [a/b][m-1]: H^m x0 (x0 = psi_n, phi), m = 1..3
+  double2* fnl[2][4] = {};       // [a/b][m]: (D/Omega) <beta|H^m x0>, m = 0..3, [nst][P]
+};
+
+static void keep_free(StepKeep& k) {
+  void* bufs[] = {k.psi, k.phi, k.pw[0][0], k.pw[0][1], k.pw[0][2], k.pw[1][0], k.pw[1][1],
+                  k.pw[1][2], k.fnl[0][0], k.fnl[0][1], k.fnl[0][2], k.fnl[0][3], k.fnl[1][0],
+                  k.fnl[1][1], k.fnl[1][2], k.fnl[1][3]};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  k = StepKeep();
+}
+
+static qbg_status keep_alloc(StepKeep& k, size_t vec_bytes, size_t fnl_bytes) {
+  std::vector<double2**> v = {&k.psi, &k.phi};
+  for (int s = 0; s < 2; ++s)
+    for (int m = 0; m < 3; ++m) v.push_back(&k.pw[s][m]);
+  for (double2** b : v) QBG_CUDA(cudaMalloc((void**)b, vec_bytes));
+  for (int s = 0; s < 2; ++s)
+    for (int m = 0; m < 4; ++m) QBG_CUDA(cudaMalloc((void**)&k.fnl[s][m], std::max<size_t>(fnl_bytes, 16)));
+  return QBG_OK;
+}
+
 struct AdjWork {
   size_t vec_bytes = 0;          // one [ld x nst] complex FP64 block
-  double2* X[3] = {};            // H^m x0, m = 1..3
   double2* Y[4] = {};            // H^j y0, j = 1..4; then M_m in Y[3-m]
   double2* chi = nullptr;        // P_b^+ lambda
-  double2* phi = nullptr; size_t phi_bytes = 0;  // P_a psi_n when the caller gives none
+  double2* lf[4] = {};           // (D/Omega) <beta|H^j y0>, j = 0..3
+  size_t lf_bytes = 0;
   double2* fields = nullptr; size_t fields_bytes = 0;  // [8][chunk][N] real space
-  double2* proj = nullptr; size_t proj_bytes = 0;      // [16][nst][P]
+  double2* proj = nullptr; size_t proj_bytes = 0;      // [12][nst][P]
   double* part = nullptr; size_t part_bytes = 0;       // block partial sums
   double* occ = nullptr; size_t occ_bytes = 0;         // per-state occupations
   std::vector<double> h_part;
+  // single-step entry point: its own forward keep and running state
+  StepKeep one;
+  double2* run = nullptr;
+  size_t one_vec = 0, one_fnl = 0;
   // derivative projector table for (A, e)
   double2* dbeta = nullptr; size_t dbeta_bytes = 0;
   void* dproj = nullptr;
-  double dA[3] = {0, 0, 0}, de[3] = {0, 0, 0};
+  double de[3] = {0, 0, 0};
+  long long dver = -1;           // plan table version the derivative was built for
   bool dvalid = false;
 };
 
 static void work_free(AdjWork* w) {
   if (!w) return;
-  void* bufs[] = {w->X[0], w->X[1], w->X[2], w->Y[0], w->Y[1], w->Y[2], w->Y[3], w->chi, w->phi,
-                  w->fields, w->proj, w->part, w->occ, w->dbeta};
+  void* bufs[] = {w->Y[0], w->Y[1], w->Y[2], w->Y[3], w->chi, w->lf[0], w->lf[1], w->lf[2],
+                  w->lf[3], w->fields, w->proj, w->part, w->occ, w->dbeta, w->run};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  keep_free(w->one);
   tc_proj_free(w->dproj);
   delete w;
 }
@@ -72,17 +112,23 @@ static AdjWork* work_of(qbg_plan* p) {
   return (AdjWork*)p->adj;
 }
 
-static qbg_status work_vectors(AdjWork* w, size_t bytes) {
-  if (w->vec_bytes >= bytes && w->chi) return QBG_OK;
-  double2** all[] = {&w->X[0], &w->X[1], &w->X[2], &w->Y[0], &w->Y[1], &w->Y[2], &w->Y[3],
-                     &w->chi};
-  size_t cur = 0;
-  for (double2** b : all) {
-    size_t c = w->vec_bytes;
-    QBG_TRY(ensure((void**)b, &c, bytes));
-    cur = c;
+static qbg_status work_vectors(qbg_plan* p, AdjWork* w, size_t bytes, int nst) {
+  const size_t fb = sizeof(double2) * (size_t)std::max(1, p->nproj) * nst;
+  if (w->vec_bytes < bytes || !w->chi) {
+    double2** all[] = {&w->Y[0], &w->Y[1], &w->Y[2], &w->Y[3], &w->chi};
+    for (double2** b : all) {
+      size_t c = w->vec_bytes;
+      QBG_TRY(ensure((void**)b, &c, bytes));
+    }
+    w->vec_bytes = bytes;
   }
-  w->vec_bytes = cur;
+  if (w->lf_bytes < fb || !w->lf[0]) {
+    for (int j = 0; j < 4; ++j) {
+      size_t c = w->lf_bytes;
+      QBG_TRY(ensure((void**)&w->lf[j], &c, fb));
+    }
+    w->lf_bytes = fb;
+  }
   return QBG_OK;
 }
 
@@ -164,24 +210,28 @@ k_grad_kin(Quad q, int ld, int ngw, const double* __restrict__ kpgx, double A0, 
   if (threadIdx.x == 0) part[(size_t)s * gridDim.x + blockIdx.x] = r;
 }
 
-// nonlocal part of dL/da from the projections pr[v][s][p]: v = m (<b|M_m>),
-// 4+m (<b|X_m>), 8+m (<b'|M_m>), 12+m (<b'|X_m>)
+// nonlocal part of dL/da: part[b] = sum over (s, p) in block b of
+//   sum_m Re(conj(dM_m) bX_m + conj(bM_m) dX_m)
+// with bM, bX the weighted projections (D/Omega)<beta|.> and dM, dX the
+// projections <beta'|.> of M_m and H^m x0, all [nst][P]
+struct NlTerms {
+  const double2* bM[4];
+  const double2* bX[4];
+  const double2* dM[4];
+  const double2* dX[4];
+};
+
 __global__ void __launch_bounds__(256)
-k_grad_nl(const double2* __restrict__ pr, int nst, int P, const double* __restrict__ wt,
-          double* __restrict__ part) {
+k_grad_nl(NlTerms t, size_t total, double* __restrict__ part) {
   __shared__ double red[256];
-  const size_t total = (size_t)nst * P;
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   double acc = 0.0;
   if (i < total) {
-    const int p = (int)(i % P);
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
-      const double2 bm = pr[(size_t)m * total + i], bx = pr[(size_t)(4 + m) * total + i];
-      const double2 dm = pr[(size_t)(8 + m) * total + i], dx = pr[(size_t)(12 + m) * total + i];
+      const double2 bm = t.bM[m][i], bx = t.bX[m][i], dm = t.dM[m][i], dx = t.dX[m][i];
       acc += (dm.x * bx.x + dm.y * bx.y) + (bm.x * dx.x + bm.y * dx.y);
     }
-    acc *= wt[p];
   }
   const double r = block_sum(acc, red);
   if (threadIdx.x == 0) part[blockIdx.x] = r;
@@ -218,20 +268,15 @@ static qbg_status field_bwd(qbg_plan* p, const double2* c, int ld, double2* f, i
   }
 }
 
-// derivative projector table for the plan's current A and direction e
+// derivative projector table for the plan's current table (A) and direction e
 static qbg_status ensure_dtable(qbg_plan* p, AdjWork* w, const double* e, cudaStream_t st) {
   if (p->nproj == 0) return QBG_OK;
-  if (w->dvalid && !memcmp(w->dA, p->A, sizeof(w->dA)) && !memcmp(w->de, e, sizeof(w->de)))
-    return QBG_OK;
+  if (w->dvalid && w->dver == p->nl_version && !memcmp(w->de, e, sizeof(w->de))) return QBG_OK;
   w->dvalid = false;
   QBG_TRY(ensure((void**)&w->dbeta, &w->dbeta_bytes, sizeof(double2) * (size_t)p->nproj * p->ngw));
   QBG_TRY(nl_build_da(p, e, w->dbeta, st));
-  if (uses_tc(p)) {
-    tc_proj_free(w->dproj);
-    w->dproj = nullptr;
-    QBG_TRY(tc_proj_build(p, w->dbeta, &w->dproj, st));
-  }
-  memcpy(w->dA, p->A, sizeof(w->dA));
+  if (uses_tc(p)) QBG_TRY(tc_proj_build(p, w->dbeta, &w->dproj, st));
+  w->dver = p->nl_version;
   memcpy(w->de, e, sizeof(w->de));
   w->dvalid = true;
   return QBG_OK;
@@ -243,20 +288,21 @@ static qbg_status project(qbg_plan* p, AdjWork* w, bool deriv, const double2* x,
   return nl_project64(p, deriv ? w->dbeta : p->d_anl, x, ld, nst, f, st);
 }
 
+// out = sum_k c_k in_k over nrows rows of cnt elements (row stride ld)
 static qbg_status comb(qbg_plan* p, const double2* const* in, const double2* c, int n, int ld,
-                       int nst, double2* out, cudaStream_t st) {
+                       int cnt, int nrows, double2* out, cudaStream_t st) {
   Comb cb;
   for (int k = 0; k < 5; ++k) {
     cb.in[k] = k < n ? in[k] : nullptr;
     cb.c[k] = k < n ? c[k] : make_double2(0.0, 0.0);
   }
   cb.n = n;
-  k_comb<<<dim3((p->ngw + 255) / 256, nst), 256, 0, st>>>(cb, ld, p->ngw, out);
+  k_comb<<<dim3((cnt + 255) / 256, nrows), 256, 0, st>>>(cb, ld, cnt, out);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
 
-static qbg_status sum_part(qbg_plan* p, AdjWork* w, size_t n, double* out, cudaStream_t st) {
+static qbg_status sum_part(AdjWork* w, size_t n, double* out, cudaStream_t st) {
   w->h_part.resize(n);
   QBG_CUDA(cudaMemcpyAsync(w->h_part.data(), w->part, sizeof(double) * n, cudaMemcpyDeviceToHost,
                            st));
@@ -264,40 +310,71 @@ static qbg_status sum_part(qbg_plan* p, AdjWork* w, size_t n, double* out, cudaS
   double s = 0.0;
   for (size_t i = 0; i < n; ++i) s += w->h_part[i];
   *out = s;
-  (void)p;
   return QBG_OK;
 }
 
-// One Taylor factor P(H(A)) of the step, with the plan's A already set:
-// y_next = P^+ y0; grad_v (device, may be null) += dL/dv and *ga (may be
-// null) += dL/da along e, for the factor that the forward applied to x0.
-static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* x0, const double2* y0,
-                             double2* y_next, int ld, int nst, const double* d_occ, double tau,
-                             const double* e, double* grad_v, double* ga, cudaStream_t st) {
-  const double2 zero = make_double2(0.0, 0.0);
-  // c_k = (-i tau)^k / k! by the recursion of the forward (factor *= -i tau / k)
-  double2 c[5];
+// c_k = (-i tau)^k / k! by the recursion of the forward (factor *= -i tau / k)
+static void taylor_coefs(double tau, double2* c) {
   c[0] = make_double2(1.0, 0.0);
   for (int k = 1; k <= 4; ++k) {
     const double m_re = -0.0 * tau / (double)k, m_im = -1.0 * tau / (double)k;
-    c[k] = make_double2(c[k - 1].x * m_re - c[k - 1].y * m_im, c[k - 1].x * m_im + c[k - 1].y * m_re);
+    c[k] = make_double2(c[k - 1].x * m_re - c[k - 1].y * m_im,
+                        c[k - 1].x * m_im + c[k - 1].y * m_re);
   }
-  double2 cc[5];
-  for (int k = 0; k <= 4; ++k) cc[k] = make_double2(c[k].x, -c[k].y);
+}
+
+// one H application with its weighted projections exported to fnl (may be null)
+static qbg_status h_apply(qbg_plan* p, const double2* in, int ld, double2* out, int nst,
+                          double2* fnl, double2* acc, double2 fac, cudaStream_t st) {
   int nb = 0;
-  const double2* xv[4] = {x0, w->X[0], w->X[1], w->X[2]};
-  for (int m = 1; m <= 3; ++m)
-    QBG_TRY(hpsi_core(p, xv[m - 1], ld, w->X[m - 1], nst, d_occ, nullptr, &nb, nullptr, 0, zero, st));
+  p->fnl_export = p->nproj > 0 ? fnl : nullptr;
+  const qbg_status s = hpsi_core(p, in, ld, out, nst, nullptr, nullptr, &nb, acc, ld, fac, st);
+  p->fnl_export = nullptr;
+  return s;
+}
+
+// psi <- P(H, tau) psi as exponential() does (same kernels, same values),
+// keeping H^1..3 psi_in in pw and (D/Omega)<beta|H^m psi_in>, m = 0..3, in fnl
+static qbg_status exp_keep(qbg_plan* p, double2* psi, int ld, int nst, double tau,
+                           double2* const* pw, double2* const* fnl, cudaStream_t st) {
+  QBG_TRY(ensure(&p->d_w[0], &p->w_bytes[0], sizeof(double2) * (size_t)ld * nst));
+  double2 c[5];
+  taylor_coefs(tau, c);
+  for (int N = 1; N <= 4; ++N) {
+    const double2* in = N == 1 ? psi : pw[N - 2];
+    double2* out = N <= 3 ? pw[N - 1] : (double2*)p->d_w[0];
+    QBG_TRY(h_apply(p, in, ld, out, nst, fnl[N - 1], psi, c[N], st));
+  }
+  return QBG_OK;
+}
+
+// forward of one step of x (psi_n in, psi_{n+1} out) keeping k
+static qbg_status forward_keep(qbg_plan* p, double2* x, int ld, int nst, double dt,
+                               const double* A_n, const double* A_np1, StepKeep& k,
+                               cudaStream_t st);
+
+// One Taylor factor P(H(A)) of the step, with the plan's A already set:
+// y_next = P^+ y0; grad_v (device, may be null) += dL/dv and *ga (may be
+// null) += dL/da along e, for the factor that the forward applied to
+// x[0] (x[1..3] = H^1..3 x0, xf[0..3] their weighted projections).
+static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* const* x,
+                             const double2* const* xf, const double2* y0, double2* y_next,
+                             int ld, int nst, double tau, const double* e, double* grad_v,
+                             double* ga, cudaStream_t st) {
+  const double2 zero = make_double2(0.0, 0.0);
+  double2 c[5], cc[5];
+  taylor_coefs(tau, c);
+  for (int k = 0; k <= 4; ++k) cc[k] = make_double2(c[k].x, -c[k].y);
   const double2* yv[5] = {y0, w->Y[0], w->Y[1], w->Y[2], w->Y[3]};
   for (int j = 1; j <= 4; ++j)
-    QBG_TRY(hpsi_core(p, yv[j - 1], ld, w->Y[j - 1], nst, d_occ, nullptr, &nb, nullptr, 0, zero, st));
-  QBG_TRY(comb(p, yv, cc, 5, ld, nst, y_next, st));
+    QBG_TRY(h_apply(p, yv[j - 1], ld, w->Y[j - 1], nst, w->lf[j - 1], nullptr, zero, st));
+  QBG_TRY(comb(p, yv, cc, 5, ld, p->ngw, nst, y_next, st));
   if (!grad_v && !ga) return QBG_OK;
   // M_m = sum_{j<=3-m} conj(c_{j+m+1}) H^j y0 into Y[3-m] (each written after its last read)
   for (int m = 0; m <= 3; ++m) {
     double2 cm[4];
     for (int j = 0; j <= 3 - m; ++j) cm[j] = cc[j + m + 1];
-    QBG_TRY(comb(p, yv, cm, 4 - m, ld, nst, w->Y[3 - m], st));
+    QBG_TRY(comb(p, yv, cm, 4 - m, ld, p->ngw, nst, w->Y[3 - m], st));
   }
   const double2* M[4] = {w->Y[3], w->Y[2], w->Y[1], w->Y[0]};
   if (grad_v) {
@@ -307,7 +384,7 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* x0, const d
       const int ns = std::min(ch, nst - s0);
       for (int m = 0; m < 4; ++m) {
         QBG_TRY(field_bwd(p, M[m] + (size_t)s0 * ld, ld, w->fields + (size_t)m * ns * p->N, ns, st));
-        QBG_TRY(field_bwd(p, xv[m] + (size_t)s0 * ld, ld, w->fields + (size_t)(4 + m) * ns * p->N,
+        QBG_TRY(field_bwd(p, x[m] + (size_t)s0 * ld, ld, w->fields + (size_t)(4 + m) * ns * p->N,
                           ns, st));
       }
       k_grad_v<<<(unsigned)((p->N + 255) / 256), 256, 0, st>>>(w->fields, ns, p->N,
@@ -319,7 +396,7 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* x0, const d
     Quad q;
     for (int m = 0; m < 4; ++m) {
       q.M[m] = M[m];
-      q.X[m] = xv[m];
+      q.X[m] = x[m];
     }
     const int gx = std::min(64, (p->ngw + 255) / 256);
     const size_t nkin = (size_t)gx * nst;
@@ -331,19 +408,30 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* x0, const d
                                              e[0], e[1], e[2], w->part);
     QBG_LAUNCHED(p);
     double skin = 0.0, snl = 0.0;
-    QBG_TRY(sum_part(p, w, nkin, &skin, st));
+    QBG_TRY(sum_part(w, nkin, &skin, st));
     if (P > 0) {
       QBG_TRY(ensure_dtable(p, w, e, st));
-      QBG_TRY(ensure((void**)&w->proj, &w->proj_bytes, sizeof(double2) * 16 * total));
+      QBG_TRY(ensure((void**)&w->proj, &w->proj_bytes, sizeof(double2) * 12 * total));
+      NlTerms t;
+      const double2* lf[4] = {w->lf[0], w->lf[1], w->lf[2], w->lf[3]};
       for (int m = 0; m < 4; ++m) {
-        QBG_TRY(project(p, w, false, M[m], ld, nst, w->proj + (size_t)m * total, st));
-        QBG_TRY(project(p, w, false, xv[m], ld, nst, w->proj + (size_t)(4 + m) * total, st));
-        QBG_TRY(project(p, w, true, M[m], ld, nst, w->proj + (size_t)(8 + m) * total, st));
-        QBG_TRY(project(p, w, true, xv[m], ld, nst, w->proj + (size_t)(12 + m) * total, st));
+        // (D/Omega)<beta|M_m> from the projections of H^j y0
+        double2 cm[4];
+        for (int j = 0; j <= 3 - m; ++j) cm[j] = cc[j + m + 1];
+        double2* bM = w->proj + (size_t)m * total;
+        QBG_TRY(comb(p, lf, cm, 4 - m, P, P, nst, bM, st));
+        double2* dM = w->proj + (size_t)(4 + m) * total;
+        double2* dX = w->proj + (size_t)(8 + m) * total;
+        QBG_TRY(project(p, w, true, M[m], ld, nst, dM, st));
+        QBG_TRY(project(p, w, true, x[m], ld, nst, dX, st));
+        t.bM[m] = bM;
+        t.bX[m] = xf[m];
+        t.dM[m] = dM;
+        t.dX[m] = dX;
       }
-      k_grad_nl<<<(unsigned)nnl, 256, 0, st>>>(w->proj, nst, P, p->d_pwt, w->part);
+      k_grad_nl<<<(unsigned)nnl, 256, 0, st>>>(t, total, w->part);
       QBG_LAUNCHED(p);
-      QBG_TRY(sum_part(p, w, nnl, &snl, st));
+      QBG_TRY(sum_part(w, nnl, &snl, st));
     }
     *ga += 2.0 * (skin + snl);
   }
@@ -353,6 +441,20 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* x0, const d
 static qbg_status set_A(qbg_plan* p, const double* A, cudaStream_t st) {
   if (A) QBG_TRY(qbg_set_vector_potential(p, A));
   return ensure_nl(p, st);
+}
+
+static qbg_status forward_keep(qbg_plan* p, double2* x, int ld, int nst, double dt,
+                               const double* A_n, const double* A_np1, StepKeep& k,
+                               cudaStream_t st) {
+  const size_t bytes = sizeof(double2) * (size_t)ld * nst;
+  QBG_CUDA(cudaMemcpyAsync(k.psi, x, bytes, cudaMemcpyDeviceToDevice, st));
+  QBG_TRY(set_A(p, A_n, st));
+  QBG_TRY(exp_keep(p, x, ld, nst, 0.5 * dt, k.pw[0], k.fnl[0], st));
+  QBG_CUDA(cudaMemcpyAsync(k.phi, x, bytes, cudaMemcpyDeviceToDevice, st));
+  QBG_TRY(set_A(p, A_np1, st));
+  QBG_TRY(exp_keep(p, x, ld, nst, 0.5 * dt, k.pw[1], k.fnl[1], st));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
+  return QBG_OK;
 }
 
 static qbg_status direct_term(qbg_plan* p, AdjWork* w, const double2* psi, int ld, int nst,
@@ -372,26 +474,22 @@ static qbg_status upload_adj_occ(AdjWork* w, const double* occ, int nst) {
   return QBG_OK;
 }
 
-// adjoint of one step: lambda <- P_a^+ P_b^+ lambda, gradients accumulated
-static qbg_status adjoint_step(qbg_plan* p, AdjWork* w, const double2* psi_n, const double2* phi_n,
-                               int ld, int nst, const double* d_occ, double dt, const double* A_n,
-                               const double* A_np1, const double* e, double2* lam,
-                               double* grad_v, double* grad_a, cudaStream_t st) {
+// adjoint of the step whose forward kept k: lambda <- P_a^+ P_b^+ lambda,
+// gradients accumulated (grad_a[0] at A_n, grad_a[1] at A_{n+1})
+static qbg_status adjoint_step(qbg_plan* p, AdjWork* w, const StepKeep& k, int ld, int nst,
+                               double dt, const double* A_n, const double* A_np1,
+                               const double* e, double2* lam, double* grad_v, double* grad_a,
+                               cudaStream_t st) {
   const double tau = 0.5 * dt;
-  if (!phi_n) {
-    QBG_TRY(set_A(p, A_n, st));
-    QBG_TRY(ensure((void**)&w->phi, &w->phi_bytes, sizeof(double2) * (size_t)ld * nst));
-    QBG_CUDA(cudaMemcpyAsync(w->phi, psi_n, sizeof(double2) * (size_t)ld * nst,
-                             cudaMemcpyDeviceToDevice, st));
-    QBG_TRY(exponential(p, w->phi, ld, nst, d_occ, tau, st));
-    phi_n = w->phi;
-  }
+  const double2* xb[4] = {k.phi, k.pw[1][0], k.pw[1][1], k.pw[1][2]};
+  const double2* fb[4] = {k.fnl[1][0], k.fnl[1][1], k.fnl[1][2], k.fnl[1][3]};
   QBG_TRY(set_A(p, A_np1, st));
-  QBG_TRY(adj_factor(p, w, phi_n, lam, w->chi, ld, nst, d_occ, tau, e, grad_v,
+  QBG_TRY(adj_factor(p, w, xb, fb, lam, w->chi, ld, nst, tau, e, grad_v,
                      grad_a ? grad_a + 1 : nullptr, st));
+  const double2* xa[4] = {k.psi, k.pw[0][0], k.pw[0][1], k.pw[0][2]};
+  const double2* fa[4] = {k.fnl[0][0], k.fnl[0][1], k.fnl[0][2], k.fnl[0][3]};
   QBG_TRY(set_A(p, A_n, st));
-  QBG_TRY(adj_factor(p, w, psi_n, w->chi, lam, ld, nst, d_occ, tau, e, grad_v,
-                     grad_a ? grad_a : nullptr, st));
+  QBG_TRY(adj_factor(p, w, xa, fa, w->chi, lam, ld, nst, tau, e, grad_v, grad_a, st));
   if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
   return QBG_OK;
 }
@@ -402,11 +500,11 @@ struct qbg_td {
   qbg_plan* p = nullptr;
   int ld = 0, nst = 0, nsteps = 0, K = 0;
   double dt = 0.0, nel = 0.0;
-  std::vector<double> occ, A;          // A: [(nsteps+1) x 3]
-  std::vector<double2*> ckpt;          // psi_n at n = 0, K, 2K, ...
-  std::vector<double2*> seg_psi, seg_phi;  // psi_n and P_a psi_n of one segment
-  double2* cur = nullptr;              // state being recomputed
-  double2* lam = nullptr;              // adjoint state
+  std::vector<double> occ, A;           // A: [(nsteps+1) x 3]
+  std::vector<double2*> ckpt;           // psi_n at n = 0, K, 2K, ...
+  std::vector<qbg::StepKeep> seg;       // what the forward of each step of a segment keeps
+  double2* cur = nullptr;               // state being recomputed
+  double2* lam = nullptr;               // adjoint state
   bool have_forward = false;
 };
 
@@ -414,9 +512,9 @@ namespace qbg {
 
 static void td_free(qbg_td* td) {
   if (!td) return;
-  for (auto* v : {&td->ckpt, &td->seg_psi, &td->seg_phi})
-    for (double2* b : *v)
-      if (b) cudaFree(b);
+  for (double2* b : td->ckpt)
+    if (b) cudaFree(b);
+  for (StepKeep& k : td->seg) keep_free(k);
   if (td->cur) cudaFree(td->cur);
   if (td->lam) cudaFree(td->lam);
   delete td;
@@ -429,16 +527,12 @@ static qbg_status copy_states(const qbg_td* td, const double2* src, double2* dst
 }
 
 // one fixed-potential ETRS step of x (the psi result equals that of
-// qbg_etrs_step with the same A_t, A_tdt); optional copies of psi_n and of
-// the half step P_a psi_n
-static qbg_status td_step(qbg_td* td, double2* x, int n, double2* psi_copy, double2* phi_copy,
-                          cudaStream_t st) {
+// qbg_etrs_step with the same A_t, A_tdt)
+static qbg_status td_step(qbg_td* td, double2* x, int n, cudaStream_t st) {
   qbg_plan* p = td->p;
   const double tau = 0.5 * td->dt;
-  if (psi_copy) QBG_TRY(copy_states(td, x, psi_copy, st));
   QBG_TRY(set_A(p, &td->A[3 * (size_t)n], st));
   QBG_TRY(exponential(p, x, td->ld, td->nst, nullptr, tau, st));
-  if (phi_copy) QBG_TRY(copy_states(td, x, phi_copy, st));
   QBG_TRY(set_A(p, &td->A[3 * (size_t)(n + 1)], st));
   QBG_TRY(exponential(p, x, td->ld, td->nst, nullptr, tau, st));
   if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
@@ -451,8 +545,8 @@ using namespace qbg;
 
 extern "C" {
 
-qbg_status qbg_etrs_adjoint_step(qbg_plan* p, const double* psi_n, const double* phi_n, int ld,
-                                 int nst, const double* occ, double dt, const double* A_n,
+qbg_status qbg_etrs_adjoint_step(qbg_plan* p, const double* psi_n, int ld, int nst,
+                                 const double* occ, double dt, const double* A_n,
                                  const double* A_np1, const double* e, double* lambda,
                                  double* grad_v, double* grad_a, void* stream) {
   QBG_TRY(check_common(p, psi_n, ld, nst, "qbg_etrs_adjoint_step"));
@@ -468,9 +562,28 @@ qbg_status qbg_etrs_adjoint_step(qbg_plan* p, const double* psi_n, const double*
   (void)occ;
   cudaStream_t st = (cudaStream_t)stream;
   AdjWork* w = work_of(p);
-  QBG_TRY(work_vectors(w, sizeof(double2) * (size_t)ld * nst));
-  return adjoint_step(p, w, (const double2*)psi_n, (const double2*)phi_n, ld, nst, nullptr, dt,
-                      A_n, A_np1, e, (double2*)lambda, grad_v, grad_a, st);
+  const size_t vb = sizeof(double2) * (size_t)ld * nst;
+  const size_t fb = sizeof(double2) * (size_t)std::max(1, p->nproj) * nst;
+  QBG_TRY(work_vectors(p, w, vb, nst));
+  if (w->one_vec < vb || w->one_fnl < fb || !w->run) {
+    keep_free(w->one);
+    if (w->run) cudaFree(w->run);
+    w->run = nullptr;
+    w->one_vec = w->one_fnl = 0;
+    const qbg_status s = keep_alloc(w->one, vb, fb);
+    if (s != QBG_OK) {
+      keep_free(w->one);
+      return s;
+    }
+    QBG_CUDA(cudaMalloc((void**)&w->run, vb));
+    w->one_vec = vb;
+    w->one_fnl = fb;
+  }
+  // the forward of the step, keeping what the adjoint needs
+  QBG_CUDA(cudaMemcpyAsync(w->run, psi_n, vb, cudaMemcpyDeviceToDevice, st));
+  QBG_TRY(forward_keep(p, w->run, ld, nst, dt, A_n, A_np1, w->one, st));
+  return adjoint_step(p, w, w->one, ld, nst, dt, A_n, A_np1, e, (double2*)lambda, grad_v, grad_a,
+                      st);
 }
 
 qbg_status qbg_td_create(qbg_plan* p, int ld, int nst, const double* occ, double dt, int nsteps,
@@ -491,14 +604,12 @@ qbg_status qbg_td_create(qbg_plan* p, int ld, int nst, const double* occ, double
   for (double o : td->occ) td->nel += o;
   td->A.assign(3 * (size_t)(nsteps + 1), 0.0);
   const size_t bytes = sizeof(double2) * (size_t)ld * nst;
+  const size_t fb = sizeof(double2) * (size_t)std::max(1, p->nproj) * nst;
   const int nseg = (nsteps + td->K - 1) / td->K;
   td->ckpt.assign(nseg, nullptr);
-  td->seg_psi.assign(td->K, nullptr);
-  td->seg_phi.assign(td->K, nullptr);
+  td->seg.assign(td->K, StepKeep());
   std::vector<double2**> all;
   for (auto& b : td->ckpt) all.push_back(&b);
-  for (auto& b : td->seg_psi) all.push_back(&b);
-  for (auto& b : td->seg_phi) all.push_back(&b);
   all.push_back(&td->cur);
   all.push_back(&td->lam);
   for (double2** b : all) {
@@ -507,6 +618,13 @@ qbg_status qbg_td_create(qbg_plan* p, int ld, int nst, const double* occ, double
       *b = nullptr;
       td_free(td);
       return cuda_status(e, "qbg_td_create");
+    }
+  }
+  for (StepKeep& k : td->seg) {
+    const qbg_status s = keep_alloc(k, bytes, fb);
+    if (s != QBG_OK) {
+      td_free(td);
+      return s;
     }
   }
   *out = td;
@@ -526,7 +644,8 @@ qbg_status qbg_td_forward(qbg_td* td, double* psi_, const double* A, double* J, 
   QBG_TRY(set_A(p, &td->A[0], st));
   if (J) QBG_TRY(qbg_current(p, psi_, td->ld, td->nst, td->occ.data(), td->nel, J, stream));
   for (int n = 0; n < td->nsteps; ++n) {
-    QBG_TRY(td_step(td, psi, n, n % td->K == 0 ? td->ckpt[n / td->K] : nullptr, nullptr, st));
+    if (n % td->K == 0) QBG_TRY(copy_states(td, psi, td->ckpt[n / td->K], st));
+    QBG_TRY(td_step(td, psi, n, st));
     if (J)
       QBG_TRY(qbg_current(p, psi_, td->ld, td->nst, td->occ.data(), td->nel,
                           J + 3 * (size_t)(n + 1), stream));
@@ -550,7 +669,7 @@ qbg_status qbg_td_backward(qbg_td* td, const double* dLdJ, const double* e, doub
   qbg_plan* p = td->p;
   AdjWork* w = work_of(p);
   const int nst = td->nst, ld = td->ld, N = td->nsteps, K = td->K;
-  QBG_TRY(work_vectors(w, sizeof(double2) * (size_t)ld * nst));
+  QBG_TRY(work_vectors(p, w, sizeof(double2) * (size_t)ld * nst, nst));
   QBG_TRY(upload_adj_occ(w, td->occ.data(), nst));
   const double zero_e[3] = {0, 0, 0};
   const double* ev = e ? e : zero_e;
@@ -566,19 +685,20 @@ qbg_status qbg_td_backward(qbg_td* td, const double* dLdJ, const double* e, doub
   const int nseg = (N + K - 1) / K;
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int s0 = seg * K, s1 = std::min(N, s0 + K);
-    // recompute the segment from its checkpoint
+    // recompute the segment from its checkpoint, keeping each step's powers
     QBG_TRY(copy_states(td, td->ckpt[seg], td->cur, st));
     for (int n = s0; n < s1; ++n)
-      QBG_TRY(td_step(td, td->cur, n, td->seg_psi[n - s0], td->seg_phi[n - s0], st));
+      QBG_TRY(forward_keep(p, td->cur, ld, nst, td->dt, &td->A[3 * (size_t)n],
+                           &td->A[3 * (size_t)(n + 1)], td->seg[n - s0], st));
     if (seg == nseg - 1) {  // cur = psi_N
       QBG_TRY(direct_term(p, w, td->cur, ld, nst, dLdJ + 3 * (size_t)N, td->lam, st));
       explicit_a(N);
     }
     for (int n = s1 - 1; n >= s0; --n) {
-      QBG_TRY(adjoint_step(p, w, td->seg_psi[n - s0], td->seg_phi[n - s0], ld, nst, nullptr,
-                           td->dt, &td->A[3 * (size_t)n], &td->A[3 * (size_t)(n + 1)],
-                           ev, td->lam, grad_v, grad_a ? grad_a + n : nullptr, st));
-      QBG_TRY(direct_term(p, w, td->seg_psi[n - s0], ld, nst, dLdJ + 3 * (size_t)n, td->lam, st));
+      QBG_TRY(adjoint_step(p, w, td->seg[n - s0], ld, nst, td->dt, &td->A[3 * (size_t)n],
+                           &td->A[3 * (size_t)(n + 1)], ev, td->lam, grad_v,
+                           grad_a ? grad_a + n : nullptr, st));
+      QBG_TRY(direct_term(p, w, td->seg[n - s0].psi, ld, nst, dLdJ + 3 * (size_t)n, td->lam, st));
       explicit_a(n);
     }
   }

@@ -104,6 +104,9 @@ struct qbg_plan {
   int* d_pl = nullptr;         // [nproj] (lm code)
   double* d_prc = nullptr;     // [nproj]
   double2* d_anl = nullptr;    // [nproj][ngw] FP64 projector table
+  size_t anl_elems = 0;        // nproj * ngw of d_anl
+  long long nl_version = 0;    // incremented by every table build
+  void* d_pdesc = nullptr;     // [nproj] projector descriptors (qbg_nl.cu)
   float2* d_anl32 = nullptr;   // [nproj][ngw] FP32 copy (mixed)
   bool nl_ready = false;
   void* tc = nullptr;          // tensor-core projector tables (mixed)
@@ -140,6 +143,8 @@ struct qbg_plan {
   bool have_ionic = false;
   bool selfconsistent = false;
   void* adj = nullptr;           // adjoint work buffers (qbg_adjoint.cu)
+  double2* fnl_export = nullptr;  // when set: receives (D/Omega)<beta|psi> [nst][nproj] of
+                                  // the next H application (device)
 };
 
 namespace qbg {
@@ -209,6 +214,7 @@ qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out,
 // tensor-core projector GEMMs (qbg_tc.cu): psi, out FP64 [ld x nst]
 qbg_status tc_build(qbg_plan* p, cudaStream_t st);
 void tc_release(qbg_plan* p);
+void tc_invalidate(qbg_plan* p);  // the table changed; buffers kept
 qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
                        const double* d_occ, double* enl_part, int* enl_blocks,
                        cudaStream_t st);

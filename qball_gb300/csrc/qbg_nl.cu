@@ -137,36 +137,52 @@ static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector
   }
 }
 
+// Builds the projector table for the plan's A.  When only A (or the atom
+// positions) changed, the table and its tensor-core pieces are rebuilt in
+// their existing buffers: no allocation, no device-wide synchronisation
+// from cudaFree on the per-step path of a laser-driven run.
 qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
   std::vector<ProjDesc> pd;
   std::vector<double> wt;
   proj_descs(p, pd, wt);
-  p->nproj = (int)pd.size();
-  tc_release(p);
-  if (p->d_ptau) cudaFree(p->d_ptau);
-  if (p->d_pwt) cudaFree(p->d_pwt);
-  if (p->d_anl) cudaFree(p->d_anl);
-  if (p->d_anl32) cudaFree(p->d_anl32);
-  p->d_ptau = nullptr;
-  p->d_pwt = nullptr;
-  p->d_anl = nullptr;
-  p->d_anl32 = nullptr;
+  const int P = (int)pd.size();
+  const size_t n = (size_t)P * p->ngw;
+  const bool same = P == p->nproj && p->d_anl && p->anl_elems == n && n > 0;
+  if (same) {
+    // kernels of any stream may still read the old table
+    QBG_CUDA(cudaDeviceSynchronize());
+    tc_invalidate(p);
+  } else {
+    tc_release(p);
+    void* bufs[] = {p->d_ptau, p->d_pwt, p->d_anl, p->d_anl32, p->d_pdesc};
+    for (void* b : bufs)
+      if (b) cudaFree(b);
+    p->d_ptau = nullptr;
+    p->d_pwt = nullptr;
+    p->d_anl = nullptr;
+    p->d_anl32 = nullptr;
+    p->d_pdesc = nullptr;
+    p->anl_elems = 0;
+  }
+  p->nproj = P;
   p->nl_ready = true;
-  if (p->nproj == 0 || p->ngw == 0) return QBG_OK;
-  ProjDesc* d_pd = nullptr;
-  QBG_CUDA(cudaMalloc(&d_pd, sizeof(ProjDesc) * pd.size()));
-  QBG_CUDA(cudaMemcpy(d_pd, pd.data(), sizeof(ProjDesc) * pd.size(), cudaMemcpyHostToDevice));
-  QBG_CUDA(cudaMalloc(&p->d_pwt, sizeof(double) * wt.size()));
-  QBG_CUDA(cudaMemcpy(p->d_pwt, wt.data(), sizeof(double) * wt.size(), cudaMemcpyHostToDevice));
-  const size_t n = (size_t)p->nproj * p->ngw;
-  QBG_CUDA(cudaMalloc(&p->d_anl, sizeof(double2) * n));
-  dim3 grid((p->ngw + 255) / 256, p->nproj);
+  p->nl_version++;
+  if (P == 0 || p->ngw == 0) return QBG_OK;
+  if (!same) {
+    QBG_CUDA(cudaMalloc(&p->d_pdesc, sizeof(ProjDesc) * P));
+    QBG_CUDA(cudaMalloc(&p->d_pwt, sizeof(double) * P));
+    QBG_CUDA(cudaMalloc(&p->d_anl, sizeof(double2) * n));
+    p->anl_elems = n;
+  }
+  // pageable host sources: these copies complete before returning
+  QBG_CUDA(cudaMemcpy(p->d_pdesc, pd.data(), sizeof(ProjDesc) * P, cudaMemcpyHostToDevice));
+  QBG_CUDA(cudaMemcpy(p->d_pwt, wt.data(), sizeof(double) * P, cudaMemcpyHostToDevice));
+  dim3 grid((p->ngw + 255) / 256, P);
   k_anl<false><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
-                                     d_pd, p->nproj, p->d_anl, nullptr);
+                                     (const ProjDesc*)p->d_pdesc, P, p->d_anl, nullptr);
   p->launches++;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFree(d_pd);
   if (e != cudaSuccess) return cuda_status(e, "k_anl");
   return QBG_OK;
 }
@@ -370,6 +386,9 @@ qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int n
                                         d_occ, (cplx<T>*)p->d_fnl, enl_part);
     QBG_LAUNCHED(p);
   }
+  if (p->fnl_export && std::is_same<T, double>::value)
+    QBG_CUDA(cudaMemcpyAsync(p->fnl_export, p->d_fnl, sizeof(double2) * total,
+                             cudaMemcpyDeviceToDevice, st));
   {
     PhaseTimer pt(p, PH_ENL_HPSI, st);
     k_nl_hpsi<T><<<dim3((p->ngw + GT - 1) / GT, nt), 256, 0, st>>>(
@@ -441,25 +460,15 @@ __global__ void k_anl_da(const double* __restrict__ kpgx, const double* __restri
 }
 
 qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_t st) {
-  std::vector<ProjDesc> pd;
-  std::vector<double> wt;
-  proj_descs(p, pd, wt);
-  if ((int)pd.size() != p->nproj) {
-    set_error("projector derivative: the projector list changed");
+  if (p->nproj == 0 || p->ngw == 0) return QBG_OK;
+  if (!p->nl_ready || !p->d_pdesc) {
+    set_error("projector derivative: the projector table is not built");
     return QBG_ERR_STATE;
   }
-  if (pd.empty() || p->ngw == 0) return QBG_OK;
-  ProjDesc* d_pd = nullptr;
-  QBG_CUDA(cudaMalloc(&d_pd, sizeof(ProjDesc) * pd.size()));
-  QBG_CUDA(cudaMemcpy(d_pd, pd.data(), sizeof(ProjDesc) * pd.size(), cudaMemcpyHostToDevice));
   dim3 grid((p->ngw + 255) / 256, p->nproj);
   k_anl_da<<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2], e[0],
-                                 e[1], e[2], d_pd, p->nproj, dbeta);
-  p->launches++;
-  cudaError_t err = cudaGetLastError();
-  if (err == cudaSuccess) err = cudaStreamSynchronize(st);
-  cudaFree(d_pd);
-  if (err != cudaSuccess) return cuda_status(err, "k_anl_da");
+                                 e[1], e[2], (const ProjDesc*)p->d_pdesc, p->nproj, dbeta);
+  QBG_LAUNCHED(p);
   return QBG_OK;
 }
 

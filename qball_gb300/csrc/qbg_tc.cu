@@ -567,6 +567,9 @@ struct TcTables {
   double* part = nullptr; size_t part_bytes = 0;
   double2* fnl = nullptr; size_t fnl_bytes = 0;
   int* status = nullptr;
+  double* pmax = nullptr;  // per-projector maxima of the table (P)
+  double* gmax = nullptr;  // per-G maxima (ngw)
+  bool stale = false;      // the table changed: re-split before the next use
 };
 
 static size_t pieces_bytes(int nRT, int nKS) { return 2ull * nRT * nKS * TC_BLOCK_BYTES; }
@@ -574,7 +577,7 @@ static size_t pieces_bytes(int nRT, int nKS) { return 2ull * nRT * nKS * TC_BLOC
 static void tc_free(TcTables* t) {
   if (!t) return;
   void* bufs[] = {t->X1, t->X2, t->s1, t->s2, t->Y, t->F, t->sY, t->sF, t->rmax, t->part, t->fnl,
-                  t->status};
+                  t->status, t->pmax, t->gmax};
   for (void* b : bufs)
     if (b) cudaFree(b);
   delete t;
@@ -585,41 +588,55 @@ void tc_release(qbg_plan* p) {
   p->tc = nullptr;
 }
 
+void tc_invalidate(qbg_plan* p) {
+  if (p->tc) ((TcTables*)p->tc)->stale = true;
+}
+
+// Split the plan's table into the FP16 pieces; the buffers of a previous
+// table of the same shape are reused (their zero padding stays valid).
 qbg_status tc_build(qbg_plan* p, cudaStream_t st) {
-  tc_release(p);
-  if (p->nproj == 0 || p->ngw == 0) return QBG_OK;
-  TcTables* t = new TcTables;
-  p->tc = t;
-  t->P = p->nproj;
-  t->ngw = p->ngw;
-  t->x1_RT = (2 * t->P + TC_M - 1) / TC_M;
-  t->x1_KS = (2 * t->ngw + TC_KS - 1) / TC_KS;
-  t->x2_RT = (2 * t->ngw + TC_M - 1) / TC_M;
-  t->x2_KS = (2 * t->P + TC_KS - 1) / TC_KS;
-  const size_t b1 = pieces_bytes(t->x1_RT, t->x1_KS), b2 = pieces_bytes(t->x2_RT, t->x2_KS);
-  QBG_CUDA(cudaMalloc(&t->X1, b1));
-  QBG_CUDA(cudaMalloc(&t->X2, b2));
-  QBG_CUDA(cudaMemsetAsync(t->X1, 0, b1, st));
-  QBG_CUDA(cudaMemsetAsync(t->X2, 0, b2, st));
-  QBG_CUDA(cudaMalloc(&t->s1, sizeof(float) * 2 * t->P));
-  QBG_CUDA(cudaMalloc(&t->s2, sizeof(float) * 2 * (size_t)t->ngw));
-  QBG_CUDA(cudaMalloc(&t->status, sizeof(int)));
+  TcTables* t = (TcTables*)p->tc;
+  if (t && (t->P != p->nproj || t->ngw != p->ngw)) {
+    tc_release(p);
+    t = nullptr;
+  }
+  if (p->nproj == 0 || p->ngw == 0) {
+    tc_release(p);
+    return QBG_OK;
+  }
+  if (!t) {
+    t = new TcTables;
+    p->tc = t;
+    t->P = p->nproj;
+    t->ngw = p->ngw;
+    t->x1_RT = (2 * t->P + TC_M - 1) / TC_M;
+    t->x1_KS = (2 * t->ngw + TC_KS - 1) / TC_KS;
+    t->x2_RT = (2 * t->ngw + TC_M - 1) / TC_M;
+    t->x2_KS = (2 * t->P + TC_KS - 1) / TC_KS;
+    const size_t b1 = pieces_bytes(t->x1_RT, t->x1_KS), b2 = pieces_bytes(t->x2_RT, t->x2_KS);
+    QBG_CUDA(cudaMalloc(&t->X1, b1));
+    QBG_CUDA(cudaMalloc(&t->X2, b2));
+    QBG_CUDA(cudaMemsetAsync(t->X1, 0, b1, st));
+    QBG_CUDA(cudaMemsetAsync(t->X2, 0, b2, st));
+    QBG_CUDA(cudaMalloc(&t->s1, sizeof(float) * 2 * t->P));
+    QBG_CUDA(cudaMalloc(&t->s2, sizeof(float) * 2 * (size_t)t->ngw));
+    QBG_CUDA(cudaMalloc(&t->status, sizeof(int)));
+    QBG_CUDA(cudaMalloc(&t->pmax, sizeof(double) * t->P));
+    QBG_CUDA(cudaMalloc(&t->gmax, sizeof(double) * t->ngw));
+  }
+  t->stale = false;
   QBG_CUDA(cudaMemsetAsync(t->status, 0, sizeof(int), st));
-  double *pmax = nullptr, *gmax = nullptr;
-  QBG_CUDA(cudaMalloc(&pmax, sizeof(double) * t->P));
-  QBG_CUDA(cudaMalloc(&gmax, sizeof(double) * t->ngw));
-  k_anl_rowmax<<<t->P, 256, 0, st>>>(p->d_anl, t->P, t->ngw, pmax);
+  k_anl_rowmax<<<t->P, 256, 0, st>>>(p->d_anl, t->P, t->ngw, t->pmax);
   QBG_LAUNCHED(p);
-  k_anl_colmax<<<(t->ngw + 255) / 256, 256, 0, st>>>(p->d_anl, t->P, t->ngw, gmax);
+  k_anl_colmax<<<(t->ngw + 255) / 256, 256, 0, st>>>(p->d_anl, t->P, t->ngw, t->gmax);
   QBG_LAUNCHED(p);
   dim3 g((t->ngw + 255) / 256, t->P);
-  k_split_x1<<<g, 256, 0, st>>>(p->d_anl, t->P, t->ngw, pmax, t->X1, t->x1_RT, t->x1_KS, t->s1);
+  k_split_x1<<<g, 256, 0, st>>>(p->d_anl, t->P, t->ngw, t->pmax, t->X1, t->x1_RT, t->x1_KS,
+                                t->s1);
   QBG_LAUNCHED(p);
-  k_split_x2<<<g, 256, 0, st>>>(p->d_anl, t->P, t->ngw, gmax, t->X2, t->x2_RT, t->x2_KS, t->s2);
+  k_split_x2<<<g, 256, 0, st>>>(p->d_anl, t->P, t->ngw, t->gmax, t->X2, t->x2_RT, t->x2_KS,
+                                t->s2);
   QBG_LAUNCHED(p);
-  QBG_CUDA(cudaStreamSynchronize(st));
-  cudaFree(pmax);
-  cudaFree(gmax);
   return QBG_OK;
 }
 
@@ -724,7 +741,7 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
                        const double* d_occ, double* enl_part, int* enl_blocks,
                        cudaStream_t st) {
   TcTables* t = (TcTables*)p->tc;
-  if (!t) QBG_TRY_TC(tc_build(p, st));
+  if (!t || t->stale) QBG_TRY_TC(tc_build(p, st));
   t = (TcTables*)p->tc;
   if (!t) return QBG_OK;
   const int P = t->P, ngw = t->ngw;
@@ -742,6 +759,9 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
     k_tc_fnl_reduce<<<rb, 256, 0, st>>>(t->part, nsplit, 2 * P, nst, p->d_pwt, d_occ, t->fnl,
                                         enl_part);
     QBG_LAUNCHED(p);
+    if (p->fnl_export)
+      QBG_CUDA(cudaMemcpyAsync(p->fnl_export, t->fnl, sizeof(double2) * total,
+                               cudaMemcpyDeviceToDevice, st));
     QBG_CUDA(cudaMemsetAsync(t->rmax, 0, sizeof(double) * nst, st));
     k_rowmax_c64<<<dim3(std::min(32, (P + 255) / 256), nst), 256, 0, st>>>(t->fnl, P, P,
                                                                          t->rmax);
@@ -776,8 +796,10 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
 // A second projector table (the derivative tables of the adjoint) in the
 // same FP16 piece layout as the plan's GEMM1 operand.
 struct TcProj {
+  int P = 0, ngw = 0;
   __half* X1 = nullptr;
   float* s1 = nullptr;
+  double* pmax = nullptr;
 };
 
 // f[n][p] = sum_z (part[z][n][2p], part[z][n][2p+1])
@@ -800,36 +822,39 @@ void tc_proj_free(void* h) {
   if (!q) return;
   if (q->X1) cudaFree(q->X1);
   if (q->s1) cudaFree(q->s1);
+  if (q->pmax) cudaFree(q->pmax);
   delete q;
 }
 
-qbg_status tc_proj_build(qbg_plan* p, const double2* table, void** out, cudaStream_t st) {
-  *out = nullptr;
+// Pieces of table (the plan's shape) into *proj, reusing its buffers when
+// the shape is unchanged.
+qbg_status tc_proj_build(qbg_plan* p, const double2* table, void** proj, cudaStream_t st) {
   TcTables* t = (TcTables*)p->tc;
-  if (!t) QBG_TRY_TC(tc_build(p, st));
+  if (!t || t->stale) QBG_TRY_TC(tc_build(p, st));
   t = (TcTables*)p->tc;
   if (!t) return QBG_OK;
-  TcProj* q = new TcProj;
-  const size_t b1 = pieces_bytes(t->x1_RT, t->x1_KS);
-  double* pmax = nullptr;
-  cudaError_t e = cudaMalloc(&q->X1, b1);
-  if (e == cudaSuccess) e = cudaMalloc(&q->s1, sizeof(float) * 2 * t->P);
-  if (e == cudaSuccess) e = cudaMalloc(&pmax, sizeof(double) * t->P);
-  if (e == cudaSuccess) e = cudaMemsetAsync(q->X1, 0, b1, st);
-  if (e == cudaSuccess) {
-    k_anl_rowmax<<<t->P, 256, 0, st>>>(table, t->P, t->ngw, pmax);
-    dim3 g((t->ngw + 255) / 256, t->P);
-    k_split_x1<<<g, 256, 0, st>>>(table, t->P, t->ngw, pmax, q->X1, t->x1_RT, t->x1_KS, q->s1);
-    p->launches += 2;
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (pmax) cudaFree(pmax);
-  if (e != cudaSuccess) {
+  TcProj* q = (TcProj*)*proj;
+  if (q && (q->P != t->P || q->ngw != t->ngw)) {
     tc_proj_free(q);
-    return cuda_status(e, "tc_proj_build");
+    q = nullptr;
+    *proj = nullptr;
   }
-  *out = q;
+  if (!q) {
+    q = new TcProj;
+    *proj = q;
+    q->P = t->P;
+    q->ngw = t->ngw;
+    const size_t b1 = pieces_bytes(t->x1_RT, t->x1_KS);
+    QBG_CUDA(cudaMalloc(&q->X1, b1));
+    QBG_CUDA(cudaMalloc(&q->s1, sizeof(float) * 2 * t->P));
+    QBG_CUDA(cudaMalloc(&q->pmax, sizeof(double) * t->P));
+    QBG_CUDA(cudaMemsetAsync(q->X1, 0, b1, st));
+  }
+  k_anl_rowmax<<<t->P, 256, 0, st>>>(table, t->P, t->ngw, q->pmax);
+  QBG_LAUNCHED(p);
+  dim3 g((t->ngw + 255) / 256, t->P);
+  k_split_x1<<<g, 256, 0, st>>>(table, t->P, t->ngw, q->pmax, q->X1, t->x1_RT, t->x1_KS, q->s1);
+  QBG_LAUNCHED(p);
   return QBG_OK;
 }
 
@@ -838,7 +863,7 @@ qbg_status tc_proj_build(qbg_plan* p, const double2* table, void** out, cudaStre
 qbg_status tc_project(qbg_plan* p, const void* proj, const double2* x, int ld, int nst,
                       double2* f, cudaStream_t st) {
   TcTables* t = (TcTables*)p->tc;
-  if (!t) QBG_TRY_TC(tc_build(p, st));
+  if (!t || t->stale) QBG_TRY_TC(tc_build(p, st));
   t = (TcTables*)p->tc;
   if (!t || nst == 0) return QBG_OK;
   const TcProj* q = (const TcProj*)proj;
