@@ -348,11 +348,6 @@ static qbg_status exp_keep(qbg_plan* p, double2* psi, int ld, int nst, double ta
   return QBG_OK;
 }
 
-// forward of one step of x (psi_n in, psi_{n+1} out) keeping k
-static qbg_status forward_keep(qbg_plan* p, double2* x, int ld, int nst, double dt,
-                               const double* A_n, const double* A_np1, StepKeep& k,
-                               cudaStream_t st);
-
 // One Taylor factor P(H(A)) of the step, with the plan's A already set:
 // y_next = P^+ y0; grad_v (device, may be null) += dL/dv and *ga (may be
 // null) += dL/da along e, for the factor that the forward applied to
@@ -443,6 +438,7 @@ static qbg_status set_A(qbg_plan* p, const double* A, cudaStream_t st) {
   return ensure_nl(p, st);
 }
 
+// forward of one step of x (psi_n in, psi_{n+1} out) keeping k
 static qbg_status forward_keep(qbg_plan* p, double2* x, int ld, int nst, double dt,
                                const double* A_n, const double* A_np1, StepKeep& k,
                                cudaStream_t st) {

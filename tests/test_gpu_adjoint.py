@@ -3,6 +3,7 @@
 - the operator pair's forward pass is the ETRS step (bitwise, currents too);
 - the adjoint step is the adjoint of the step: <lam, S x> = <S^+ lam, x>
   (FP64, 1e-12);
+- FP64 gradients equal the CPU oracle adjoint (oracle/adjoint.py, 1e-8);
 - dL/dv(r) and dL/d(pulse amplitudes) of a dipole loss over a laser-driven
   run agree with central finite differences of the FP64 forward (1e-6);
 - the gradients do not depend on the checkpoint interval (1e-13);
@@ -178,3 +179,29 @@ def test_operator_pair_state_errors(cuda):
     with pytest.raises(Q.QbgError, match="no forward"):
         td.backward(np.zeros((3, 3)))
     td.close()
+
+
+def test_gradients_match_oracle_adjoint(cuda):
+    """FP64 operator pair against the CPU oracle's adjoint (oracle/adjoint.py)
+    on the same seeded 3-state run of the 12-bohr cell."""
+    from oracle import oracle as O
+    from oracle.adjoint import TDAdjoint
+    N, nst = 3, 3
+    cell, H, v, _, _ = setup("t12", "fp64")
+    b = Q.Basis(cell.L, cell.ecut)
+    psi_h = synth.wavefunctions(cell, b, nst=nst)
+    occ = synth.occupations(cell, nst=nst)
+    ak, G = laser(N, nk=3)
+    dstar = ad.target_dipole(N, scale=2e-3)
+    L, gv, gk = _grads(H, dev(psi_h), occ, ak, G, N, 2, dstar)
+    ob = O.Basis(b.a, cell.ecut)
+    oft = O.FT(ob, *cell.grid)
+    td = TDAdjoint(ob, oft, v, synth.species(cell), occ, DT)
+    A = potential(ak, G)
+    states, J = td.forward(np.asfortranarray(psi_h.T), A)
+    Lo, gJ = ad.loss_and_dJ(J, DT, dstar)
+    gvo, gao, _ = td.backward(states, A, gJ, E)
+    gko = ad.grad_amplitudes(gao, G)
+    assert abs(L - Lo) < 1e-10 * abs(Lo)
+    assert rel_err(gv, gvo) < 1e-8, rel_err(gv, gvo)
+    assert rel_err(gk, gko) < 1e-8, rel_err(gk, gko)
