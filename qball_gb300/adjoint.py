@@ -86,6 +86,46 @@ def grad_amplitudes(grad_a, G):
     return -(G.T @ grad_a)
 
 
+def _sum_over_ranks(x):
+    """In-place sum over the ranks of the default process group of a numpy
+    array or torch tensor (host arrays travel through the device under NCCL)."""
+    import torch
+    import torch.distributed as dist
+    if torch.is_tensor(x):
+        dist.all_reduce(x)
+        return x
+    t = torch.from_numpy(x)
+    if dist.get_backend() == "nccl":
+        d = t.cuda()
+        dist.all_reduce(d)
+        t.copy_(d.cpu())
+    else:
+        dist.all_reduce(t)
+    return x
+
+
+def dipole_loss_gradients(op, psi, A, dt, dstar, e, grad_v=None):
+    """One forward and backward pass of the dipole loss through the operator
+    pair op (TDPropagation: forward(psi, A) -> J, backward(dLdJ, e, grad_v)
+    -> dL/da_n).  When a process group of several ranks is initialised, each
+    rank holds a block of the states: the step currents are summed over the
+    ranks before the loss (J is a sum over states, the reference's
+    Context::dsum at CurrentDensity.cc:86-92), and dL/dv(r) and dL/da_n after
+    the backward pass (sums over states).  Returns (L, J, dL/da_n)."""
+    import torch.distributed as dist
+    sharded = dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1
+    J = op.forward(psi, A)
+    if sharded:
+        _sum_over_ranks(J)
+    L, gJ = loss_and_dJ(J, dt, dstar)
+    ga = op.backward(gJ, e=e, grad_v=grad_v)
+    if sharded:
+        _sum_over_ranks(ga)
+        if grad_v is not None:
+            _sum_over_ranks(grad_v)
+    return L, J, ga
+
+
 def main():
     sys.path.insert(0, os.path.dirname(HERE))
     import torch
