@@ -417,9 +417,20 @@ extern "C" {
 const char* qbg_last_error(void) { return g_err.c_str(); }
 const char* qbg_version(void) { return "qball-gb300 0.1 (sm_103a)"; }
 
+// a right-handed cell of positive volume (UnitCell::volume() > 0)
+static bool cell_ok(const double* a) {
+  double b[9], vol;
+  cell_b(a, b, &vol);
+  return vol > 0.0 && std::isfinite(vol);
+}
+
 qbg_status qbg_basis_dims(const double* a, double ecut, int* info) {
   if (!a || !info || !(ecut >= 0.0)) {
     set_error("qbg_basis_dims: null argument or negative ecut");
+    return QBG_ERR_INVALID;
+  }
+  if (!cell_ok(a)) {
+    set_error("qbg_basis_dims: the cell vectors span no positive volume");
     return QBG_ERR_INVALID;
   }
   build_rods(a, ecut, info);
@@ -431,6 +442,10 @@ qbg_status qbg_basis_fill(const double* a, double ecut, int* rod_h, int* rod_k,
                           double* kpgx) {
   if (!a || !(ecut >= 0.0)) {
     set_error("qbg_basis_fill: null cell or negative ecut");
+    return QBG_ERR_INVALID;
+  }
+  if (!cell_ok(a)) {
+    set_error("qbg_basis_fill: the cell vectors span no positive volume");
     return QBG_ERR_INVALID;
   }
   int info[12];
