@@ -274,7 +274,10 @@ qbg_status qbg_etrs_adjoint_step(qbg_plan* plan, const double* psi_n, int ld,
  * pass recomputes each segment of K steps from its checkpoint, keeping per
  * step psi_n, the half step, the Taylor powers H^1..3 of both and their
  * projections (8 state-sized buffers per step, 8K in all), and runs the
- * adjoint steps in reverse: 16 H applications per step in all. */
+ * adjoint steps in reverse: 16 H applications per step in all.  The
+ * operator pair borrows the plan (which must outlive it, as Basis must
+ * outlive FourierTransform in the reference) and uses the plan's stream
+ * rules: one operator pair or plan call at a time per plan. */
 typedef struct qbg_td qbg_td;
 qbg_status qbg_td_create(qbg_plan* plan, int ld, int nst, const double* occ,
                          double dt, int nsteps, int K, qbg_td** td);
