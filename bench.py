@@ -306,9 +306,21 @@ def roofline_of(H, cell, basis, prof, peaks, nst):
     unit = ("TFLOP/s (FFMA-equivalent: 2 x FP32-pipe instructions of the double-float "
             "algorithm per second)" if H.precision == "mixed_df32" and dom.startswith("ft_")
             else "TFLOP/s")
+    per_launch_ms = tot_ms / max(nl, 1)
+    hbm_view = None
+    if traffic:
+        # the same launches against the measured HBM copy bandwidth: DRAM
+        # bytes per launch (ncu) over the live per-launch time
+        hbm_peak = float(peaks.get("hbm_gbs", 6785.5))
+        hbm_gbs = traffic / (per_launch_ms / 1000.0) / 1e9
+        hbm_view = {"bound": "hbm", "achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": hbm_gbs / hbm_peak,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks
+                    else "fallback 6785.5 GB/s"}
     return {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
+            "hbm_view": hbm_view,
             "unit": unit, "frac": achieved / peak, "traffic": traffic,
-            "per_launch_ms": tot_ms / max(nl, 1), "launches_per_H": nl,
+            "per_launch_ms": per_launch_ms, "launches_per_H": nl,
             "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 kind::f16 runs at the same "
                             "rate)" if bound == "tensor" else "profiles/peaks_gb300.txt"),
             "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
