@@ -42,6 +42,27 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 
 METRIC = "TDDFT ETRS steps/s (216 at.) mixed vs FP64 GPU at <=1e-8 dipole rel err"
+
+
+def workload_config(cfg, cell, ngw, ngv, dt, hxc):
+    """The `config` object of both arms: the workload and its Hamiltonian."""
+    return {"workload": f"{cfg}: {cell.natoms} atoms, L={cell.L:g} bohr, ecut {2 * cell.ecut:g} Ry, "
+                        f"grid {cell.grid[0]}^3, {ngw} PW (full sphere), {cell.nst} states, "
+                        f"{nproj_of(cell)} KB projectors, ETRS dt={dt}, delta kick A_z=0.01",
+            "hamiltonian": (f"self-consistent: v_ion + Hartree + LDA rebuilt from the density of "
+                            f"psi(t) and of the predicted psi(t+dt) every step, density sphere "
+                            f"{2 * synth_density_ecut(cell):g} Ry ({ngv} G)" if hxc else
+                            "fixed local potential")}
+
+
+def synth_density_ecut(cell):
+    from qball_gb300 import synth
+    return synth.density_ecut(cell)
+
+
+def metric_for(cell):
+    """The metric's name with the atom count of the cell actually timed."""
+    return METRIC.replace("(216 at.)", f"({cell.natoms} at.)")
 UNIT = "steps/s"
 
 
@@ -59,6 +80,9 @@ def parse():
     ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--cpu-states", type=int, default=16)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--fp64-simt-steps", type=int, default=0,
+                    help="ETRS steps of the FP64 form with FP64-FMA projector GEMMs (0: one "
+                         "profiled H|psi> only; a step takes ~40 s on the 216-atom cell)")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--chunk", type=int, default=0)
@@ -170,46 +194,8 @@ def make_system(cfg, precision, psi_np=None, chunk=0):
     H.set_vlocal(synth.vlocal(cell))
     H.set_nonlocal(synth.species(cell))
     if psi_np is None:
-        psi_np = make_psi(cell, basis)
+        psi_np = synth.device_wavefunctions(cell, basis)
     return cell, basis, H, psi_np
-
-
-def enable_hxc(H, cell, p, occ):
-    """Density basis, ionic terms, v_r of the density of p, and the
-    self-consistent step (EhrenSampleStepper.cc:322-329 before the first
-    step).  Returns the density basis size."""
-    import torch
-    import qball_gb300 as Q
-    from qball_gb300 import synth
-    vb = Q.Basis(cell.L, synth.density_ecut(cell))
-    vion, rhopst = synth.ionic_terms(cell, vb)
-    H.set_density_basis(vb)
-    H.set_ionic_terms(vion, rhopst)
-    rho = torch.empty(H.n012, dtype=torch.float64, device=p.device)
-    H.update_density(p, occ, rho)
-    H.update_vhxc(rho)
-    H.set_selfconsistent(True)
-    del rho
-    return vb
-
-
-def make_psi(cell, basis):
-    """Seeded random states, Gram-orthonormalised in FP64 (the nst x nst
-    factor on the host, the products on the device)."""
-    import torch
-    rng = np.random.default_rng(cell.seed + 7)
-    n, ngw = cell.nst, basis.ngw
-    env = torch.from_numpy(np.exp(-basis.kpg2 / 8.0)).cuda()
-    c = torch.empty((n, ngw), dtype=torch.complex128, device="cuda")
-    for s0 in range(0, n, 64):
-        s1 = min(n, s0 + 64)
-        blk = rng.standard_normal((s1 - s0, ngw)) + 1j * rng.standard_normal((s1 - s0, ngw))
-        c[s0:s1] = torch.from_numpy(blk).cuda() * env
-    # Gram factor on the host (nst x nst): c <- conj(L)^-1 c with S = L L^H
-    S = (c.conj() @ c.T).cpu().numpy()
-    L = np.linalg.cholesky(S)
-    Linv = np.linalg.inv(np.conj(L))
-    return torch.from_numpy(Linv).cuda() @ c
 
 
 def time_etrs(H, p, occ, dt, A, steps, warmup, stream):
@@ -245,6 +231,14 @@ def _df32_inst(n):
     return DF32_INST_PER_LINE.get(n, _fft_flops(n) * 18480.0 / _fft_flops(120))
 
 
+def arith_peaks():
+    """FP32 FFMA and FP64 DFMA peaks (TFLOP/s) measured on the GB300s
+    (profiles/peaks_gb300.json)."""
+    with open(os.path.join(HERE, "profiles", "peaks_gb300.json")) as f:
+        pk = json.load(f)
+    return float(pk["fp32_ffma_tflops"]), float(pk["fp64_dfma_tflops"])
+
+
 def phase_model(H, cell, basis):
     """Algorithmic work per STATE of each timed phase: (amount, bound, peak).
 
@@ -259,13 +253,19 @@ def phase_model(H, cell, basis):
     nband = 2 * (max(abs(basis.idxmin[1]), abs(basis.idxmax[1])) + 1)
     P = nproj_of(cell)
     prec = H.precision
+    f32, f64 = arith_peaks()
     if prec == "mixed_df32":
-        w, fb = (lambda n: 2.0 * _df32_inst(n)), ("fp32", 72.2)
+        w, fb = (lambda n: 2.0 * _df32_inst(n)), ("fp32", f32)
     elif prec in ("fp64", "mixed_fft64"):
-        w, fb = _fft_flops, ("fp64", 1.007)
+        w, fb = _fft_flops, ("fp64", f64)
     else:
-        w, fb = _fft_flops, ("fp32", 72.2)
+        w, fb = _fft_flops, ("fp32", f32)
     tc = prec in ("mixed", "mixed_fft64", "mixed_df32")
+    # executed slice products per real GEMM on the tensor pipe: 3 (2-piece
+    # FP16 split) in the mixed forms; Ozaki slices S in the FP64 form:
+    # S (S + 1) / 2 pairs
+    oz = prec == "fp64" and getattr(H, "fp64_gemm", "simt") == "ozaki"
+    nprod = 3 if tc else (H.oz_slices * (H.oz_slices + 1) // 2 if oz else 1)
     lines = {
         "ft_z_bwd": nrods * w(n2),
         "ft_z_fwd": nrods * w(n2),
@@ -277,7 +277,7 @@ def phase_model(H, cell, basis):
     }
     m = {k: (v, fb) for k, v in lines.items()}
     gemm = 8.0 * P * ngw  # one complex GEMM, per state
-    m["fnl_gemm"] = (3 * gemm if tc else gemm, ("tensor", None) if tc else ("fp64", 1.007))
+    m["fnl_gemm"] = (nprod * gemm, ("tensor", None) if (tc or oz) else ("fp64", f64))
     m["enl_hpsi"] = m["fnl_gemm"]
     return m
 
@@ -322,7 +322,7 @@ def roofline_of(H, cell, basis, prof, peaks, nst):
             "unit": unit, "frac": achieved / peak, "traffic": traffic,
             "per_launch_ms": per_launch_ms, "launches_per_H": nl,
             "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 kind::f16 runs at the same "
-                            "rate)" if bound == "tensor" else "profiles/peaks_gb300.txt"),
+                            "rate)" if bound == "tensor" else "profiles/peaks_gb300.json"),
             "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
             "phase_frac_of_peak": {k: round(model[k][0] * nst / (v[0] / 1000.0) / 1e12 /
                                             (float(peaks.get("bf16_tflops", 1917.4))
@@ -394,22 +394,32 @@ def run_reference(args, rank, world):
             vals.append(res["value"])
     v = float(np.median(vals))
     res["value"] = v
-    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": K, "warmup": W, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"{args.config}: 216-atom cell, L=30, 50 Ry, 120^3, 432 states, "
-                                   f"ETRS dt={args.dt}, sampled on {args.cpu_states} states"},
+    from oracle import oracle as O
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    cell = synth.make_cell(args.config)
+    hxc = args.hxc == "on"
+    ngw = O.Basis(Q.cubic_cell(cell.L), cell.ecut).ngw
+    ngv = O.Basis(Q.cubic_cell(cell.L), synth.density_ecut(cell)).ngw if hxc else 0
+    line = {"impl": "reference", "metric": metric_for(cell), "value": v, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": K, "warmup": W, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(args.config, cell, ngw, ngv, args.dt, hxc),
             "cpu_baseline": res,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def accuracy_table():
+def accuracy_table(cfg):
+    """Measured 200-step dipole errors of each form against the FP64 form for
+    the cell `cfg` (profiles/accuracy.json, python -m qball_gb300.accuracy);
+    {} when that cell was not measured."""
     try:
         a = json.load(open(os.path.join(HERE, "profiles", "accuracy.json")))
-        return a.get("c2_216atoms_16states", {})
     except (OSError, ValueError):
         return {}
+    ent = a.get("by_config", {}).get(cfg, {})
+    return ent.get("forms", {})
 
 
 def run_ours(args, rank, world, local):
@@ -422,13 +432,13 @@ def run_ours(args, rank, world, local):
         peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
     except (OSError, ValueError):
         pass
-    acc = accuracy_table()
+    acc = accuracy_table(args.config)
     cell, basis, H, psi = make_system(args.config, args.form, chunk=args.chunk)
     occ = synth.occupations(cell)
     A = synth.kick()
     H.set_vector_potential(A)
     hxc = args.hxc == "on"
-    vb = enable_hxc(H, cell, psi, occ) if hxc else None
+    vb = synth.enable_selfconsistent(H, cell, psi, occ) if hxc else None
     p = psi.clone()
     barrier(world)
     clocks = Clocks(local)
@@ -517,25 +527,32 @@ def run_ours(args, rank, world, local):
 
     # the other forms on the same cell and states
     others = {}
-    runs = [(f, args.also_steps, args.also_warmup) for f in args.also.split(",") if f]
-    runs.append(("fp64", args.fp64_steps, args.fp64_warmup))
-    for form, steps, warm in runs:
-        if not form or (form == "fp64" and args.skip_fp64):
-            continue
+    # (label, form, FP64 GEMM, steps, warm-up); 0 steps: one profiled H|psi> only
+    runs = [(f, f, None, args.also_steps, args.also_warmup) for f in args.also.split(",") if f]
+    if not args.skip_fp64:
+        runs.append(("fp64", "fp64", "ozaki", args.fp64_steps, args.fp64_warmup))
+        runs.append(("fp64_simt", "fp64", "simt", args.fp64_simt_steps, args.fp64_warmup
+                     if args.fp64_simt_steps else 0))
+    for label, form, gemm, steps, warm in runs:
         _, _, H2, _ = make_system(args.config, form, psi_np=psi)
+        if gemm:
+            H2.set_fp64_gemm(gemm)
         H2.set_vector_potential(A)
         if hxc:
-            enable_hxc(H2, cell, psi, occ)
+            synth.enable_selfconsistent(H2, cell, psi, occ)
         p2 = psi.clone()
-        ms2, _ = time_etrs(H2, p2, occ, args.dt, A, steps, warm, stream)
-        ms2 = allreduce_max(ms2, world)
+        ent = {"unit": UNIT, "steps": steps, "warmup": warm,
+               "dipole_rel_err_200_steps": acc.get(label)}
+        if steps:
+            ms2, _ = time_etrs(H2, p2, occ, args.dt, A, steps, warm, stream)
+            ms2 = allreduce_max(ms2, world)
+            ent["value"] = world * steps / (ms2 / 1000.0)
         H2.profile(True)
         H2.hpsi(p2, hp, occ, stream=stream)
         pr2 = H2.profile_read()
         H2.profile(False)
-        others[form] = {"value": world * steps / (ms2 / 1000.0), "unit": UNIT, "steps": steps,
-                        "warmup": warm, "dipole_rel_err_200_steps": acc.get(form),
-                        "phases_ms_per_H": {k: round(v[0], 3) for k, v in pr2.items() if v[1]}}
+        ent["phases_ms_per_H"] = {k: round(v[0], 3) for k, v in pr2.items() if v[1]}
+        others[label] = ent
         del H2, p2
         torch.cuda.empty_cache()
 
@@ -552,30 +569,24 @@ def run_ours(args, rank, world, local):
                            "FP32 accumulate per 256, compensated), FP64 kinetic/Taylor/reductions",
             "mixed": "FP32 transforms, tensor-core projector GEMMs (FP16 2-piece split), FP64 "
                      "kinetic/Taylor/reductions",
-            "fp64": "FP64 throughout"}
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "fp64": "FP64 throughout; projector GEMMs FP64-accurate on the tensor cores "
+                    "(Ozaki scheme: 7 slices of 7 bits, exact FP32 windows)",
+            "fp64_simt": "FP64 throughout; projector GEMMs as FP64 FMAs on the CUDA cores"}
+        line = {"metric": metric_for(cell), "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64 + f16-split tensor GEMM" if args.form != "fp64" else "f64",
                 "form": args.form, "form_desc": form_desc.get(args.form, args.form),
                 "dipole_rel_err_200_steps": acc.get(args.form),
                 "data": "synthetic (seeded cell, random orthonormal states)",
-                "config": {"workload": f"{args.config}: {cell.natoms} atoms, L={cell.L:g} bohr, "
-                                       f"ecut {2 * cell.ecut:g} Ry, grid "
-                                       f"{cell.grid[0]}^3, {basis.ngw} PW (full sphere), "
-                                       f"{cell.nst} states, {nproj_of(cell)} KB projectors, "
-                                       f"ETRS dt={args.dt}, delta kick A_z=0.01",
-                           "hamiltonian": (f"self-consistent: v_ion + Hartree + LDA rebuilt from "
-                                           f"the density of psi(t) and of the predicted "
-                                           f"psi(t+dt) every step, density sphere "
-                                           f"{2 * vb.ecut:g} Ry ({vb.ngw} G)" if hxc else
-                                           "fixed local potential"),
+                "config": {**workload_config(args.config, cell, basis.ngw,
+                                             vb.ngw if hxc else 0, args.dt, hxc),
                            "l2": f"inputs (psi {psi.numel() * 16 / 1e9:.1f} GB) larger than L2; "
                                  "no flush",
                            "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"},
                 "gpu_launches": launches, "clocks": clk, "roofline": roofline,
                 "e2e": e2e, "other_forms": others, "cpu_baseline": cpu}
-        if "fp64" in others:
+        if "value" in others.get("fp64", {}):
             line["speedup_vs_fp64_gpu"] = value / others["fp64"]["value"]
         print(json.dumps(line), flush=True)
 

@@ -21,7 +21,12 @@
  *  - All array arguments of compute entry points are DEVICE pointers unless
  *    the parameter comment says "host".  Calls are asynchronous on the given
  *    CUDA stream (NULL = legacy default stream) unless they return a host
- *    scalar, in which case they synchronise that stream first.
+ *    scalar, in which case they synchronise that stream first.  Calls that
+ *    run tensor-core GEMMs (qbg_hpsi, qbg_etrs_step and the adjoint in the
+ *    forms that use them) also synchronise the given stream before they
+ *    return: they read the GEMMs' error word on that stream, so a bounded
+ *    wait that expired is reported by the call that ran it
+ *    (QBG_ERR_TIMEOUT).
  *  - Every function returns a qbg_status; no C++ exception crosses the ABI.
  *    qbg_last_error() gives a message for the last failure on this thread.
  *  - A plan is thread-compatible, not thread-safe: one plan per stream at a
@@ -58,6 +63,15 @@ enum {
                                transforms: ~48-bit, on the FP32 pipe; the
                                kinetic term and Taylor increment are
                                double-float products added to FP64 */
+};
+
+/* Projector GEMMs of the plain FP64 form (qbg_plan_set_fp64_gemm). */
+enum {
+  QBG_GEMM_SIMT = 0,  /* FP64 FMA on the CUDA cores */
+  QBG_GEMM_OZAKI = 1  /* FP64-accurate on the tensor cores (the default): the
+                         Ozaki scheme, operands split into 7-bit integer
+                         slices (FP16, exact), slice products accumulated
+                         exactly in FP32 tensor memory over windows of K */
 };
 
 typedef struct qbg_plan qbg_plan;
@@ -100,6 +114,15 @@ qbg_status qbg_plan_create(const qbg_basis_desc* basis, int np0, int np1,
 qbg_status qbg_plan_destroy(qbg_plan* plan);
 /* states processed per transform launch group (L2 working-set control) */
 qbg_status qbg_plan_set_chunk(qbg_plan* plan, int states_per_chunk);
+/* How the plain FP64 form (precision QBG_PREC_FP64) runs the two complex
+ * GEMMs of NonLocalPotential::energy (NonLocalPotential.cc:2064, 2165):
+ * QBG_GEMM_OZAKI (default) on the tensor cores with every row scaled by a
+ * power of two and written as `slices` balanced 7-bit digits (7: 49 bits,
+ * 6: 42 bits; the digit products of equal weight summed exactly), or
+ * QBG_GEMM_SIMT with FP64 FMAs.  Both match FP64 to rounding level of the
+ * row maxima; the tensor-core form is ~70x faster on GB300, whose FP64 pipe
+ * runs at 1/72 of FP32.  Other forms ignore the setting. */
+qbg_status qbg_plan_set_fp64_gemm(qbg_plan* plan, int mode, int slices);
 
 /* FourierTransform::backward(c, f) (FourierTransform.cc:529), batched over
  * nbatch states: c [ldc x nbatch] complex, f [N x nbatch] complex (FP64). */
@@ -115,10 +138,11 @@ qbg_status qbg_backward(qbg_plan* plan, const double* c, int ldc, double* f,
  * intermediates, 16*np2*(nrods + nband*np0) bytes with nband =
  * 2*(max|k|+1), must fit in 32 MiB, else QBG_ERR_INVALID.  The first call
  * on a device resolves the array's device address (make that first call
- * before any stream capture).  Calls share the array: two calls whose
- * kernels overlap on the GPU race, so serialise them (one stream).  The
- * array needs no clearing (every element read is first written by the same
- * call). */
+ * before any stream capture).  The address is kept for the life of the
+ * process: no cudaDeviceReset of that device may come between calls.  Calls
+ * share the array: two calls whose kernels overlap on the GPU race, so
+ * serialise them (one stream).  The array needs no clearing (every element
+ * read is first written by the same call). */
 qbg_status qbg_backward_noalloc(qbg_plan* plan, const double* c, int ldc,
                                 double* f, int nbatch, void* stream);
 
@@ -331,6 +355,14 @@ qbg_status qbg_plan_autotune(qbg_plan* plan, const double* psi, int ld, int nst,
  * it gives up as designed -- the path every wait of the tensor-core kernel
  * takes instead of hanging.  The device stays usable.  Synchronises. */
 qbg_status qbg_selftest_wait_timeout(int polls);
+
+/* Diagnostic, no reference counterpart: poll limit of the pipeline waits of
+ * this plan's tensor-core GEMMs (-1 restores the default, ~0.2 s; 0 makes
+ * every such wait give up at once).  The waits for a CTA's own copies and
+ * MMAs to land before it frees its memory keep the default limit, so an
+ * expired wait ends the launch cleanly: the call that ran it returns
+ * QBG_ERR_TIMEOUT and the plan stays usable.  For tests of that path. */
+qbg_status qbg_plan_set_wait_polls(qbg_plan* plan, int polls);
 
 /* ---- Instrumentation (no reference counterpart beyond its TimerMap,
  *      NonLocalPotential.cc:54, EhrenSampleStepper.cc:1136-1149) ------- */

@@ -4,10 +4,18 @@
 # UnitCell.cc, functionals/LDAFunctional.cc), compiled in place from the read-only reference tree, plus the
 # one-process Context stub and the C shim in this folder.  The reference's
 # build system is not used.  Test infrastructure only.
+#
+#   build_ref.sh [REFERENCE_ROOT]     (or QBG_REFERENCE=REFERENCE_ROOT build_ref.sh)
+#
+# Without a reference root, or where its sources are absent, nothing is built.
 set -e
-REF=${QBG_REFERENCE:-/root/reference}
+REF=${1:-${QBG_REFERENCE:-}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
+if [ -z "$REF" ]; then
+  echo "build_ref.sh: no reference root given (argument or QBG_REFERENCE); skipping" >&2
+  exit 0
+fi
 if [ ! -f "$REF/src/qball/FourierTransform.cc" ]; then
   echo "build_ref.sh: reference sources not found under $REF; skipping" >&2
   exit 0

@@ -33,6 +33,8 @@ QBG_PREC_MIXED = 1
 QBG_PREC_MIXED_FFT64 = 2
 QBG_PREC_MIXED_NL64 = 3
 QBG_PREC_MIXED_DF32 = 4
+QBG_GEMM_SIMT = 0
+QBG_GEMM_OZAKI = 1
 PRECISIONS = {"fp64": QBG_PREC_FP64, "mixed": QBG_PREC_MIXED,
               "mixed_fft64": QBG_PREC_MIXED_FFT64, "mixed_nl64": QBG_PREC_MIXED_NL64,
               "mixed_df32": QBG_PREC_MIXED_DF32}
@@ -52,6 +54,7 @@ ABI = {
     "qbg_plan_create": [_P, _I, _I, _I, _I, _P],
     "qbg_plan_destroy": [_P],
     "qbg_plan_set_chunk": [_P, _I],
+    "qbg_plan_set_fp64_gemm": [_P, _I, _I],
     "qbg_backward": [_P, _P, _I, _P, _I, _P],
     "qbg_backward_noalloc": [_P, _P, _I, _P, _I, _P],
     "qbg_forward": [_P, _P, _P, _I, _I, _P],
@@ -79,6 +82,7 @@ ABI = {
     "qbg_etrs_graph_destroy": [_P],
     "qbg_plan_autotune": [_P, _P, _I, _I, _P, _P, _P],
     "qbg_selftest_wait_timeout": [_I],
+    "qbg_plan_set_wait_polls": [_P, _I],
     "qbg_launch_count": [_P, _P],
     "qbg_profile": [_P, _I],
     "qbg_profile_read": [_P, _P, _P, _I],
@@ -198,6 +202,7 @@ class FourierTransform:
                                      ctypes.byref(h)), "qbg_plan_create")
         self.h = h
         self.chunk = 32  # plan default
+        self.fp64_gemm, self.oz_slices = "ozaki", 7  # plan default
 
     def close(self):
         if getattr(self, "h", None):
@@ -229,9 +234,22 @@ class FourierTransform:
         self.chunk = ch.value
         return ch.value
 
+    def set_fp64_gemm(self, mode="ozaki", slices=7):
+        """Projector GEMMs of the plain FP64 form: "ozaki" (FP64-accurate on
+        the tensor cores, `slices` 7-bit digit planes, the default) or
+        "simt" (FP64 FMAs)."""
+        m = {"simt": QBG_GEMM_SIMT, "ozaki": QBG_GEMM_OZAKI}[mode]
+        _check(lib().qbg_plan_set_fp64_gemm(self.h, m, int(slices)), "qbg_plan_set_fp64_gemm")
+        self.fp64_gemm, self.oz_slices = mode, int(slices)
+
     def set_chunk(self, n):
         _check(lib().qbg_plan_set_chunk(self.h, int(n)), "qbg_plan_set_chunk")
         self.chunk = int(n)
+
+    def set_wait_polls(self, polls=-1):
+        """Poll limit of the tensor-core GEMMs' pipeline waits (-1: default;
+        0: every such wait expires at once, for tests of the timeout path)."""
+        _check(lib().qbg_plan_set_wait_polls(self.h, int(polls)), "qbg_plan_set_wait_polls")
 
     def launches(self):
         c = ctypes.c_longlong()

@@ -25,7 +25,6 @@ def run_form(precision, cell, basis, psi0, occ, A, dt, steps, chunk=0, hxc=True)
     import torch
     import qball_gb300 as Q
     from qball_gb300 import synth
-    from bench import enable_hxc
     H = Q.Hamiltonian(basis, *cell.grid, precision=precision)
     if chunk:
         H.set_chunk(chunk)
@@ -33,7 +32,7 @@ def run_form(precision, cell, basis, psi0, occ, A, dt, steps, chunk=0, hxc=True)
     H.set_nonlocal(synth.species(cell))
     H.set_vector_potential(A)
     if hxc:
-        enable_hxc(H, cell, psi0, occ)
+        synth.enable_selfconsistent(H, cell, psi0, occ)
     p = psi0.clone()
     nel = float(occ.sum())
     J = [H.current(p, occ, nel)]
@@ -56,7 +55,6 @@ def main():
     import qball_gb300 as Q
     from qball_gb300 import synth
     sys.path.insert(0, os.path.dirname(HERE))
-    from bench import make_psi  # seeded state generator shared with bench.py
 
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2")
@@ -72,7 +70,7 @@ def main():
     kw = {"nst": args.nst} if args.nst else {}
     cell = synth.make_cell(args.config, **kw)
     basis = Q.Basis(cell.L, cell.ecut)
-    psi0 = make_psi(cell, basis)
+    psi0 = synth.device_wavefunctions(cell, basis)
     occ = synth.occupations(cell)
     A = synth.kick()
     res = {}

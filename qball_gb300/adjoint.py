@@ -131,7 +131,6 @@ def main():
     import torch
     import qball_gb300 as Q
     from qball_gb300 import synth
-    from bench import make_psi
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2")
     ap.add_argument("--form", default="mixed_df32")
@@ -148,7 +147,7 @@ def main():
     H = Q.Hamiltonian(b, *cell.grid, precision=args.form)
     H.set_vlocal(synth.vlocal(cell))
     H.set_nonlocal(synth.species(cell))
-    psi0 = make_psi(cell, b)
+    psi0 = synth.device_wavefunctions(cell, b)
     occ = synth.occupations(cell)
     N, dt = args.steps, args.dt
     times = dt * np.arange(N + 1)

@@ -449,7 +449,7 @@ static qbg_status forward_keep(qbg_plan* p, double2* x, int ld, int nst, double 
   QBG_CUDA(cudaMemcpyAsync(k.phi, x, bytes, cudaMemcpyDeviceToDevice, st));
   QBG_TRY(set_A(p, A_np1, st));
   QBG_TRY(exp_keep(p, x, ld, nst, 0.5 * dt, k.pw[1], k.fnl[1], st));
-  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p, st));
   return QBG_OK;
 }
 
@@ -486,7 +486,7 @@ static qbg_status adjoint_step(qbg_plan* p, AdjWork* w, const StepKeep& k, int l
   const double2* fa[4] = {k.fnl[0][0], k.fnl[0][1], k.fnl[0][2], k.fnl[0][3]};
   QBG_TRY(set_A(p, A_n, st));
   QBG_TRY(adj_factor(p, w, xa, fa, w->chi, lam, ld, nst, tau, e, grad_v, grad_a, st));
-  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p, st));
   return QBG_OK;
 }
 
@@ -531,7 +531,7 @@ static qbg_status td_step(qbg_td* td, double2* x, int n, cudaStream_t st) {
   QBG_TRY(exponential(p, x, td->ld, td->nst, nullptr, tau, st));
   QBG_TRY(set_A(p, &td->A[3 * (size_t)(n + 1)], st));
   QBG_TRY(exponential(p, x, td->ld, td->nst, nullptr, tau, st));
-  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p, st));
   return QBG_OK;
 }
 

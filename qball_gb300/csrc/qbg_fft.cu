@@ -881,51 +881,58 @@ static bool big_prime(const LenTables& L) {
   return false;
 }
 
+// The launchers below work on the plan's Z and Y intermediates unless the
+// caller passes its own (Z, Y: the same shapes for ns states).
 template <typename T, bool BIGP>
-static qbg_status run_z_bwd_(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st) {
+static qbg_status run_z_bwd_(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st,
+                             void* Z) {
   const FFTLen<T> d = p->len[2].view<T>();
   const size_t sm = smem_bytes<T>(d, false, nthreads_z(d));
   QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   PhaseTimer pt(p, PH_Z_BWD, st);
-  k_z_bwd<T, BIGP><<<grid, nthreads_z(d), sm, st>>>(c, ldc, (cplx<T>*)p->d_Z, p->d_rods, p->nrods, d);
+  k_z_bwd<T, BIGP><<<grid, nthreads_z(d), sm, st>>>(c, ldc, (cplx<T>*)(Z ? Z : p->d_Z), p->d_rods,
+                                                    p->nrods, d);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
 template <typename T>
-static qbg_status run_z_bwd(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st) {
-  return big_prime(p->len[2]) ? run_z_bwd_<T, true>(p, c, ldc, ns, st)
-                              : run_z_bwd_<T, false>(p, c, ldc, ns, st);
+static qbg_status run_z_bwd(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st,
+                            void* Z = nullptr) {
+  return big_prime(p->len[2]) ? run_z_bwd_<T, true>(p, c, ldc, ns, st, Z)
+                              : run_z_bwd_<T, false>(p, c, ldc, ns, st, Z);
 }
 
 template <typename T, bool BIGP>
-static qbg_status run_x_(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
+static qbg_status run_x_(qbg_plan* p, bool bwd, int ns, cudaStream_t st, void* Z, void* Y) {
   const FFTLen<T> d = p->len[0].view<T>();
   const size_t sm = smem_bytes<T>(d);
   dim3 grid(p->np2 * ((p->nband + kTile - 1) / kTile), ns);
+  cplx<T>* z = (cplx<T>*)(Z ? Z : p->d_Z);
+  cplx<T>* y = (cplx<T>*)(Y ? Y : p->d_Y);
   PhaseTimer pt(p, bwd ? PH_X_BWD : PH_X_FWD, st);
   if (bwd) {
     QBG_CUDA(prep(k_x_bwd<T, BIGP>, sm));
-    k_x_bwd<T, BIGP><<<grid, nthreads(d), sm, st>>>((const cplx<T>*)p->d_Z, (cplx<T>*)p->d_Y, p->nrods,
-                                           p->nband, p->np2, p->d_row_ptr, p->d_row_rod,
-                                           p->d_row_x, d);
+    k_x_bwd<T, BIGP><<<grid, nthreads(d), sm, st>>>(z, y, p->nrods, p->nband, p->np2,
+                                                    p->d_row_ptr, p->d_row_rod, p->d_row_x, d);
   } else {
     QBG_CUDA(prep(k_x_fwd<T, BIGP>, sm));
-    k_x_fwd<T, BIGP><<<grid, nthreads(d), sm, st>>>((const cplx<T>*)p->d_Y, (cplx<T>*)p->d_Z, p->nrods,
-                                           p->nband, p->np2, p->d_row_ptr, p->d_row_rod,
-                                           p->d_row_x, d);
+    k_x_fwd<T, BIGP><<<grid, nthreads(d), sm, st>>>(y, z, p->nrods, p->nband, p->np2,
+                                                    p->d_row_ptr, p->d_row_rod, p->d_row_x, d);
   }
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
 template <typename T>
-static qbg_status run_x(qbg_plan* p, bool bwd, int ns, cudaStream_t st) {
-  return big_prime(p->len[0]) ? run_x_<T, true>(p, bwd, ns, st) : run_x_<T, false>(p, bwd, ns, st);
+static qbg_status run_x(qbg_plan* p, bool bwd, int ns, cudaStream_t st, void* Z = nullptr,
+                        void* Y = nullptr) {
+  return big_prime(p->len[0]) ? run_x_<T, true>(p, bwd, ns, st, Z, Y)
+                              : run_x_<T, false>(p, bwd, ns, st, Z, Y);
 }
 
 template <typename T, int MODE, bool BIGP>
 static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, double* rho,
-                         int rho_acc, cudaStream_t st) {
+                         int rho_acc, cudaStream_t st, void* Y = nullptr) {
   const FFTLen<T> d = p->len[1].view<T>();
   const size_t sm = smem_bytes<T>(d, MODE == Y_VLOC);
   QBG_CUDA(prep(k_y<T, MODE, BIGP>, sm));
@@ -937,8 +944,9 @@ static qbg_status run_y_(qbg_plan* p, int ns, double2* f, const double* w, doubl
     v = std::is_same<T, double>::value  ? (const T*)p->d_vr
         : std::is_same<T, float>::value ? (const T*)p->d_vr32
                                         : (const T*)p->d_vrdf;
-  k_y<T, MODE, BIGP><<<grid, nthreads(d), sm, st>>>((cplx<T>*)p->d_Y, p->nband, p->np0, p->np2,
-                                                p->d_band_y, v, f, w, ns, rho, rho_acc, d);
+  k_y<T, MODE, BIGP><<<grid, nthreads(d), sm, st>>>((cplx<T>*)(Y ? Y : p->d_Y), p->nband,
+                                                    p->np0, p->np2, p->d_band_y, v, f, w, ns,
+                                                    rho, rho_acc, d);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
@@ -1224,47 +1232,21 @@ qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst, const double
 
 // Backward transform with caller-provided scratch (Z for chunk*n2*nrods,
 // Y for chunk*n2*nband*n0 complex elements of type T); allocates nothing.
-template <typename T, bool BX, bool BY, bool BZ>
-static qbg_status backward_scratch_(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,
-                                    cplx<T>* Z, cplx<T>* Y, int chunk, cudaStream_t st) {
-  const FFTLen<T> dz = p->len[2].view<T>(), dx = p->len[0].view<T>(), dy = p->len[1].view<T>();
-  const size_t smz = smem_bytes<T>(dz), smx = smem_bytes<T>(dx), smy = smem_bytes<T>(dy);
-  QBG_CUDA(prep(k_z_bwd<T, BZ>, smz));
-  QBG_CUDA(prep(k_x_bwd<T, BX>, smx));
-  QBG_CUDA((prep(k_y<T, Y_BWD_STORE, BY>, smy)));
-  for (int s0 = 0; s0 < nb; s0 += chunk) {
-    const int ns = std::min(chunk, nb - s0);
-    k_z_bwd<T, BZ><<<dim3((p->nrods + kTile - 1) / kTile, ns), kThreads, smz, st>>>(
-        c + (size_t)s0 * ldc, ldc, Z, p->d_rods, p->nrods, dz);
-    QBG_LAUNCHED(p);
-    k_x_bwd<T, BX><<<dim3(p->np2 * ((p->nband + kTile - 1) / kTile), ns), kThreads, smx, st>>>(
-        Z, Y, p->nrods, p->nband, p->np2, p->d_row_ptr, p->d_row_rod, p->d_row_x, dx);
-    QBG_LAUNCHED(p);
-    k_y<T, Y_BWD_STORE, BY><<<dim3(p->np2 * ((p->np0 + kTile - 1) / kTile), ns), kThreads, smy,
-                              st>>>(Y, p->nband, p->np0, p->np2, p->d_band_y, nullptr,
-                                    f + (size_t)s0 * p->N, nullptr, ns, nullptr, 0, dy);
-    QBG_LAUNCHED(p);
-  }
-  return QBG_OK;
-}
-
+// The same launchers (thread counts, shared memory) as backward().
 template <typename T>
 qbg_status backward_scratch(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,
                             void* Z, void* Y, int chunk, cudaStream_t st) {
-  const bool bx = big_prime(p->len[0]), by = big_prime(p->len[1]), bz = big_prime(p->len[2]);
-  cplx<T>* z = (cplx<T>*)Z;
-  cplx<T>* y = (cplx<T>*)Y;
-  // the three lengths are dispatched independently
-  if (bx) {
-    if (by) return bz ? backward_scratch_<T, true, true, true>(p, c, ldc, f, nb, z, y, chunk, st)
-                      : backward_scratch_<T, true, true, false>(p, c, ldc, f, nb, z, y, chunk, st);
-    return bz ? backward_scratch_<T, true, false, true>(p, c, ldc, f, nb, z, y, chunk, st)
-              : backward_scratch_<T, true, false, false>(p, c, ldc, f, nb, z, y, chunk, st);
+  for (int s0 = 0; s0 < nb; s0 += chunk) {
+    const int ns = std::min(chunk, nb - s0);
+    QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ldc, ldc, ns, st, Z));
+    QBG_TRY(run_x<T>(p, true, ns, st, Z, Y));
+    QBG_TRY(big_prime(p->len[1])
+                ? (run_y_<T, Y_BWD_STORE, true>(p, ns, f + (size_t)s0 * p->N, nullptr, nullptr,
+                                                0, st, Y))
+                : (run_y_<T, Y_BWD_STORE, false>(p, ns, f + (size_t)s0 * p->N, nullptr, nullptr,
+                                                 0, st, Y)));
   }
-  if (by) return bz ? backward_scratch_<T, false, true, true>(p, c, ldc, f, nb, z, y, chunk, st)
-                    : backward_scratch_<T, false, true, false>(p, c, ldc, f, nb, z, y, chunk, st);
-  return bz ? backward_scratch_<T, false, false, true>(p, c, ldc, f, nb, z, y, chunk, st)
-            : backward_scratch_<T, false, false, false>(p, c, ldc, f, nb, z, y, chunk, st);
+  return QBG_OK;
 }
 
 template qbg_status backward_scratch<double>(qbg_plan*, const double2*, int, double2*, int, void*,

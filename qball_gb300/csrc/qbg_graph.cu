@@ -164,7 +164,7 @@ qbg_status qbg_etrs_graph_check(qbg_graph* g) {
     return QBG_ERR_INVALID;
   }
   QBG_CUDA(cudaDeviceSynchronize());
-  for (qbg_plan* p : g->plans) QBG_TRY(tc_check_status(p));
+  for (qbg_plan* p : g->plans) QBG_TRY(tc_check_status(p, nullptr));
   return QBG_OK;
 }
 

@@ -110,7 +110,11 @@ struct qbg_plan {
   float2* d_anl32 = nullptr;   // [nproj][ngw] FP32 copy (mixed)
   bool nl_ready = false;
   void* tc = nullptr;          // tensor-core projector tables (mixed)
+  void* oz = nullptr;          // FP64-accurate tensor-core projector tables (plain form)
+  int fp64_gemm = QBG_GEMM_OZAKI;  // projector GEMMs of the plain FP64 form
+  int oz_slices = 7;           // 7-bit slices per operand of those GEMMs (6 or 7)
   bool check_every_step = true; // read the tensor-core status word after each step
+  int tc_polls = -1;            // poll limit of the GEMM pipeline waits (-1: default)
   bool lane_fft = true;         // register-resident lane-group transforms where supported
   bool fuse_xyx = true;         // x, y and x passes of H psi in one kernel where they fit
 
@@ -218,7 +222,15 @@ void tc_invalidate(qbg_plan* p);  // the table changed; buffers kept
 qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
                        const double* d_occ, double* enl_part, int* enl_blocks,
                        cudaStream_t st);
-qbg_status tc_check_status(qbg_plan* p);
+qbg_status tc_check_status(qbg_plan* p, cudaStream_t st);
+
+// FP64-accurate (Ozaki-scheme) tensor-core projector GEMMs (qbg_ozaki.cu)
+qbg_status oz_build(qbg_plan* p, cudaStream_t st);
+void oz_release(qbg_plan* p);
+void oz_invalidate(qbg_plan* p);
+qbg_status oz_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, int nst,
+                       const double* d_occ, double* enl_part, int* enl_blocks, cudaStream_t st);
+qbg_status oz_check_status(qbg_plan* p, cudaStream_t st);
 
 // misc kernels (qbg_ops.cu)
 qbg_status update_kinetic(qbg_plan* p, cudaStream_t st);

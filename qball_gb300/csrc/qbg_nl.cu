@@ -152,8 +152,10 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
     // kernels of any stream may still read the old table
     QBG_CUDA(cudaDeviceSynchronize());
     tc_invalidate(p);
+    oz_invalidate(p);
   } else {
     tc_release(p);
+    oz_release(p);
     void* bufs[] = {p->d_ptau, p->d_pwt, p->d_anl, p->d_anl32, p->d_pdesc};
     for (void* b : bufs)
       if (b) cudaFree(b);

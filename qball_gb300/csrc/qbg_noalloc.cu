@@ -27,7 +27,8 @@ static void* g_noalloc_ptr[kMaxDevices];  // device address of the array, per de
 
 // Device address of the static array on the current device.  The first call
 // on a device resolves it with cudaGetSymbolAddress (host code cannot use the
-// array's name as a device pointer).
+// array's name as a device pointer) and keeps it for the life of the process,
+// so the device must not be reset (cudaDeviceReset) between calls.
 static qbg_status noalloc_scratch(void** out) {
   int dev = 0;
   QBG_CUDA(cudaGetDevice(&dev));

@@ -119,8 +119,12 @@ qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* out, int 
   *enl_blocks = 0;
   if (p->prec == QBG_PREC_FP64) {
     if (nl) {
-      QBG_TRY(nl_apply<double>(p, psi, ld, out, nst, d_occ, enl_part, st));
-      *enl_blocks = nl_reduce_blocks(p, nst);
+      if (p->fp64_gemm == QBG_GEMM_OZAKI) {
+        QBG_TRY(oz_nl_apply(p, psi, ld, out, nst, d_occ, enl_part, enl_blocks, st));
+      } else {
+        QBG_TRY(nl_apply<double>(p, psi, ld, out, nst, d_occ, enl_part, st));
+        *enl_blocks = nl_reduce_blocks(p, nst);
+      }
     }
     return local_hpsi<double>(p, psi, ld, out, nst, nl, acc, ldacc, fac, st);
   }
@@ -141,7 +145,8 @@ qbg_status hpsi_core(qbg_plan* p, const double2* psi, int ld, double2* out, int 
 
 bool uses_tc(const qbg_plan* p) {
   return p->prec == QBG_PREC_MIXED || p->prec == QBG_PREC_MIXED_FFT64 ||
-         p->prec == QBG_PREC_MIXED_DF32;
+         p->prec == QBG_PREC_MIXED_DF32 ||
+         (p->prec == QBG_PREC_FP64 && p->fp64_gemm == QBG_GEMM_OZAKI);
 }
 
 qbg_status check_common(qbg_plan* p, const void* a, int ld, int nst, const char* who) {
@@ -305,7 +310,7 @@ qbg_status qbg_hpsi(qbg_plan* p, const double* psi, int ld, double* hpsi, int ns
   int nb = 0;
   QBG_TRY(hpsi_core(p, (const double2*)psi, ld, (double2*)hpsi, nst, d_occ,
                     enl ? p->d_red : nullptr, &nb, nullptr, 0, zero, st));
-  if (uses_tc(p)) QBG_TRY(tc_check_status(p));
+  if (uses_tc(p)) QBG_TRY(tc_check_status(p, st));
   if (enl) {
     *enl = 0.0;
     if (nb > 0) {
@@ -439,7 +444,7 @@ qbg_status qbg_etrs_step(qbg_plan* p, double* psi_, int ld, int nst, const doubl
   }
   if (A_tdt) QBG_TRY(qbg_set_vector_potential(p, A_tdt));
   QBG_TRY(exponential(p, psi, ld, nst, d_occ, dt1, st));
-  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p));
+  if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p, st));
   return QBG_OK;
 }
 

@@ -485,6 +485,7 @@ qbg_status qbg_plan_destroy(qbg_plan* p) {
   if (!p) return QBG_OK;
   adj_release(p);
   tc_release(p);
+  oz_release(p);
   hxc_release(p);
   for (auto& L : p->len) free_len(L);
   void* bufs[] = {p->d_rods, p->d_row_ptr, p->d_row_rod, p->d_row_x, p->d_band_y,
@@ -627,6 +628,31 @@ qbg_status qbg_plan_set_chunk(qbg_plan* p, int states) {
     return QBG_ERR_INVALID;
   }
   p->chunk = states;
+  return QBG_OK;
+}
+
+qbg_status qbg_plan_set_fp64_gemm(qbg_plan* p, int mode, int slices) {
+  if (!p || (mode != QBG_GEMM_SIMT && mode != QBG_GEMM_OZAKI) ||
+      (mode == QBG_GEMM_OZAKI && slices != 6 && slices != 7)) {
+    set_error("qbg_plan_set_fp64_gemm: mode must be QBG_GEMM_SIMT or QBG_GEMM_OZAKI with 6 or "
+              "7 slices");
+    return QBG_ERR_INVALID;
+  }
+  if (mode != p->fp64_gemm || (mode == QBG_GEMM_OZAKI && slices != p->oz_slices)) {
+    QBG_CUDA(cudaDeviceSynchronize());  // kernels may still read the old slices
+    oz_release(p);
+  }
+  p->fp64_gemm = mode;
+  if (mode == QBG_GEMM_OZAKI) p->oz_slices = slices;
+  return QBG_OK;
+}
+
+qbg_status qbg_plan_set_wait_polls(qbg_plan* p, int polls) {
+  if (!p || polls < -1 || polls > (1 << 21)) {
+    set_error("qbg_plan_set_wait_polls: polls must be -1 (default) or in [0, 2^21]");
+    return QBG_ERR_INVALID;
+  }
+  p->tc_polls = polls;
   return QBG_OK;
 }
 

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "qbg_internal.h"
+#include "qbg_tcgen05.cuh"
 
 namespace qbg {
 
@@ -58,7 +59,6 @@ constexpr int TC_THREADS = 576;    // producer, MMA issuer, 16 epilogue warps
 constexpr int TC_NBUF = 4;         // tensor-memory chunk buffers (4 x 128 columns)
 constexpr int TC_EPI = 512;        // epilogue threads
 constexpr int TC_ECOLS = 32;       // columns per epilogue thread
-constexpr int TC_SPIN = 1 << 21;   // polls per bounded wait (~0.2 s with backoff)
 
 // byte offset of element (r, k) inside one 128x32 block image
 __host__ __device__ __forceinline__ int tc_canon(int r, int k) {
@@ -231,89 +231,6 @@ __global__ void k_split_rows4(const double2* __restrict__ x, int ld, int ncols,
   *reinterpret_cast<uint4*>(Y + tc_index(1, n, 2 * g0, nRT, nKS)) = *reinterpret_cast<uint4*>(lo);
 }
 
-// ------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t su32(const void* p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count));
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
-}
-// bounded wait for the phase with parity `par` to complete; false on timeout
-// or when another CTA has already raised the grid-wide error word
-__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t par, const int* gstatus,
-                                          int limit = TC_SPIN) {
-  for (int it = 0; it < limit; ++it) {
-    uint32_t ok;
-    asm volatile(
-        "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        "selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(su32(b)), "r"(par)
-        : "memory");
-    if (ok) return true;
-    if (it > 64) __nanosleep(64);
-    if ((it & 4095) == 4095 && *(volatile const int*)gstatus) return false;
-  }
-  return false;
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          su32(dst)),
-      "l"(src), "r"(bytes), "r"(su32(bar))
-      : "memory");
-}
-__device__ __forceinline__ uint64_t sdesc(uint32_t addr) {
-  // no-swizzle K-major canonical layout: LBO (K direction) 128 B, SBO (8-row
-  // groups) 256 B, descriptor version 1
-  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) |
-         ((uint64_t)(256 >> 4) << 32) | ((uint64_t)1 << 46);
-}
-__device__ __forceinline__ uint32_t idesc_f16_f32(int m, int n) {
-  // D F32 (bit 4), A/B F16 (format 0), K-major, N>>3 at bit 17, M>>4 at 24
-  return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc,
-                                        uint32_t acc) {
-  asm volatile(
-      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-      "l"(da), "l"(db), "r"(idesc), "r"(acc));
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-      su32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tmem_ld32(uint32_t ta, uint32_t* r) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(ta));
-}
-__device__ __forceinline__ void tmem_st32(uint32_t ta, const uint32_t* r) {
-  asm volatile(
-      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(ta),
-      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
-      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
-      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
-      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
-      "r"(r[29]), "r"(r[30]), "r"(r[31]));
-}
-
 // epilogue modes
 enum { TC_OUT_PARTIAL = 0, TC_OUT_HPSI = 1 };
 
@@ -328,6 +245,7 @@ struct TcArgs {
   double* out;      // PARTIAL: [split][N][M] doubles; HPSI: complex out, real view
   int ldo;          // HPSI: leading dimension of out in complex elements
   int* status;      // error word (1 = a bounded wait expired)
+  int polls;        // poll limit of the pipeline waits (the drains always use TC_SPIN)
 };
 
 template <int MODE>
@@ -374,8 +292,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tbase = *tmem_slot;
-  // tensor memory columns: [0,128) chunk buffer 0, [128,256) buffer 1,
-  // [256,384) running sum hi, [384,512) running sum lo
+  // tensor memory columns: four chunk buffers of 128 columns; the running
+  // sums live in the epilogue threads' registers
   if (nks > 0) {
     if (warp == 0 && lane == 0) {
       // ---------------- producer
@@ -385,7 +303,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       for (int i = 0; i < nks; ++i) {
         const int s = i % TC_STAGES;
         const uint32_t par = ((i / TC_STAGES) & 1) ^ 1;
-        if (i >= TC_STAGES && !mbar_wait(&empty[s], par, args.status)) {
+        if (i >= TC_STAGES && !mbar_wait(&empty[s], par, args.status, args.polls)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
           break;
@@ -403,14 +321,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       }
       // no copy may still be landing in shared memory when the CTA retires
       for (int i = max(0, issued - TC_STAGES); i < issued; ++i)
-        mbar_wait(&full[i % TC_STAGES], (i / TC_STAGES) & 1, args.status);
+        if (!mbar_wait_drain(&full[i % TC_STAGES], (i / TC_STAGES) & 1)) {
+          *abort_flag = 1;
+          atomicExch(args.status, 1);
+        }
     } else if (warp == 1 && lane == 0) {
       // ---------------- MMA issuer
       const uint32_t idesc = idesc_f16_f32(TC_M, TC_N);
       int i = 0;
       for (int c = 0; c < nchunks && !*abort_flag; ++c) {
         const int b = c % TC_NBUF;
-        if (c >= TC_NBUF && !mbar_wait(&accempty[b], ((c / TC_NBUF) - 1) & 1, args.status)) {
+        if (c >= TC_NBUF &&
+            !mbar_wait(&accempty[b], ((c / TC_NBUF) - 1) & 1, args.status, args.polls)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
           break;
@@ -421,7 +343,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
         bool first = true;
         for (; i < iend; ++i) {
           const int s = i % TC_STAGES;
-          if (!mbar_wait(&full[s], (i / TC_STAGES) & 1, args.status)) {
+          if (!mbar_wait(&full[s], (i / TC_STAGES) & 1, args.status, args.polls)) {
             *abort_flag = 1;
             atomicExch(args.status, 1);
             break;
@@ -441,12 +363,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
           }
           mma_commit(&empty[s]);  // frees the stage once these MMAs are done
         }
+        if (*abort_flag) break;  // nobody folds this chunk; the drain below tracks its MMAs
         mma_commit(&accfull[b]);
-        if (*abort_flag) break;
       }
       // every MMA of this thread has completed before tensor memory is freed
       mma_commit(drain);
-      mbar_wait(drain, 0, args.status);
+      if (!mbar_wait_drain(drain, 0)) {
+        *abort_flag = 1;
+        atomicExch(args.status, 1);
+      }
     } else if (warp >= 2) {
       // ---------------- epilogue: fold each chunk into compensated (hi, lo)
       // sums held in registers.  Warp w reads tensor-memory lane quarter
@@ -463,7 +388,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
       bool ok = true;
       for (int c = 0; c < nchunks; ++c) {
         const int b = c % TC_NBUF;
-        if (!mbar_wait(&accfull[b], (c / TC_NBUF) & 1, args.status)) {
+        if (!mbar_wait(&accfull[b], (c / TC_NBUF) & 1, args.status, args.polls)) {
           *abort_flag = 1;
           atomicExch(args.status, 1);
           ok = false;
@@ -489,7 +414,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         mbar_arrive(&accempty[b]);
       }
-      // final write from the registers
+      // final write from the registers, once the MMA thread's drain has
+      // completed (every MMA of the tile is done)
+      if (ok && !mbar_wait_drain(drain, 0)) {
+        *abort_flag = 1;
+        atomicExch(args.status, 1);
+        ok = false;
+      }
       if (ok && !*abort_flag) {
         const int m = mt * TC_M + q * 32 + lane;
         if (m < args.M) {
@@ -567,6 +498,7 @@ struct TcTables {
   double* part = nullptr; size_t part_bytes = 0;
   double2* fnl = nullptr; size_t fnl_bytes = 0;
   int* status = nullptr;
+  int* h_status = nullptr; // pinned host copy of the error word
   double* pmax = nullptr;  // per-projector maxima of the table (P)
   double* gmax = nullptr;  // per-G maxima (ngw)
   bool stale = false;      // the table changed: re-split before the next use
@@ -580,6 +512,7 @@ static void tc_free(TcTables* t) {
                   t->status, t->pmax, t->gmax};
   for (void* b : bufs)
     if (b) cudaFree(b);
+  if (t->h_status) cudaFreeHost(t->h_status);
   delete t;
 }
 
@@ -727,6 +660,7 @@ static qbg_status tc_gemm1(qbg_plan* p, TcTables* t, const __half* X1, const flo
   a1.out = t->part;
   a1.ldo = 0;
   a1.status = t->status;
+  a1.polls = p->tc_polls >= 0 ? p->tc_polls : TC_SPIN;
   {
     PhaseTimer pt(p, PH_FNL_GEMM, st);
     QBG_TRY_TC(tc_launch(p, TC_OUT_PARTIAL, a1, mt1, nRT, nsplit, st));
@@ -785,6 +719,7 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
   a2.out = (double*)out;
   a2.ldo = ld;
   a2.status = t->status;
+  a2.polls = p->tc_polls >= 0 ? p->tc_polls : TC_SPIN;
   {
     PhaseTimer pt(p, PH_ENL_HPSI, st);
     QBG_TRY_TC(tc_launch(p, TC_OUT_HPSI, a2, t->x2_RT, nRT, 1, st));
@@ -887,14 +822,25 @@ __global__ void k_wait_selftest(int polls, int* status) {
   }
 }
 
-qbg_status tc_check_status(qbg_plan* p) {
+// Reads the error word on the caller's stream (ordered after the launches
+// it covers) into pinned host memory and synchronises that stream; a raised
+// word is cleared on the same stream and reported as QBG_ERR_TIMEOUT.
+qbg_status tc_check_status(qbg_plan* p, cudaStream_t st) {
+  if (p->oz) {
+    const qbg_status s = oz_check_status(p, st);
+    if (s != QBG_OK) return s;
+  }
   TcTables* t = (TcTables*)p->tc;
   if (!t) return QBG_OK;
-  int s = 0;
-  QBG_CUDA(cudaMemcpy(&s, t->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!t->h_status) QBG_CUDA(cudaMallocHost(&t->h_status, sizeof(int)));
+  *t->h_status = 0;
+  QBG_CUDA(cudaMemcpyAsync(t->h_status, t->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  QBG_CUDA(cudaStreamSynchronize(st));
+  const int s = *t->h_status;
   if (s) {
     set_error("tensor-core GEMM: a bounded wait expired (status %d)", s);
-    cudaMemset(t->status, 0, sizeof(int));
+    QBG_CUDA(cudaMemsetAsync(t->status, 0, sizeof(int), st));
+    QBG_CUDA(cudaStreamSynchronize(st));
     return QBG_ERR_TIMEOUT;
   }
   return QBG_OK;

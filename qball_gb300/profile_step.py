@@ -55,8 +55,7 @@ def main():
     A = synth.kick()
     H.set_vector_potential(A)
     if args.hxc == "on":
-        from bench import enable_hxc
-        enable_hxc(H, cell, psi, occ)
+            synth.enable_selfconsistent(H, cell, psi, occ)
     out = torch.zeros_like(psi)
     for _ in range(args.hpsi):
         H.hpsi(psi, out, occ)

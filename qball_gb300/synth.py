@@ -184,3 +184,42 @@ def ionic_terms(cell, vbasis, depth=-2.0, width=1.0, rcps=1.0, zv=None):
     vion = depth * (2.0 * np.pi * width * width) ** 1.5 * np.exp(-0.5 * g2 * width * width) * S / om
     rhopst = -zv * np.exp(-0.25 * g2 * rcps * rcps) * S / om
     return vion, rhopst
+
+
+def enable_selfconsistent(H, cell, p, occ):
+    """Density basis, ionic terms and v_r of the density of the device
+    states p on the Hamiltonian H, then the self-consistent step
+    (EhrenSampleStepper.cc:322-329 before the first step).  Returns the
+    density basis."""
+    import torch
+    import qball_gb300 as Q
+    vb = Q.Basis(cell.L, density_ecut(cell))
+    vion, rhopst = ionic_terms(cell, vb)
+    H.set_density_basis(vb)
+    H.set_ionic_terms(vion, rhopst)
+    rho = torch.empty(H.n012, dtype=torch.float64, device=p.device)
+    H.update_density(p, occ, rho)
+    H.update_vhxc(rho)
+    H.set_selfconsistent(True)
+    del rho
+    return vb
+
+
+def device_wavefunctions(cell, basis, nst=None):
+    """Seeded random states on cuda, Gram-orthonormalised in FP64: the
+    nst x nst Cholesky factor on the host, the products on the device
+    (torch complex128 [nst, ngw])."""
+    import torch
+    rng = np.random.default_rng(cell.seed + 7)
+    n, ngw = (cell.nst if nst is None else nst), basis.ngw
+    env = torch.from_numpy(np.exp(-basis.kpg2 / 8.0)).cuda()
+    c = torch.empty((n, ngw), dtype=torch.complex128, device="cuda")
+    for s0 in range(0, n, 64):
+        s1 = min(n, s0 + 64)
+        blk = rng.standard_normal((s1 - s0, ngw)) + 1j * rng.standard_normal((s1 - s0, ngw))
+        c[s0:s1] = torch.from_numpy(blk).cuda() * env
+    # c <- conj(L)^-1 c with S = L L^H
+    S = (c.conj() @ c.T).cpu().numpy()
+    L = np.linalg.cholesky(S)
+    Linv = np.linalg.inv(np.conj(L))
+    return torch.from_numpy(Linv).cuda() @ c

@@ -105,3 +105,28 @@ def test_bounded_wait_expires_and_context_survives(cuda):
     H.hpsi(dev(psi), out, occ)
     torch.cuda.synchronize()
     assert torch.isfinite(out.abs()).all()
+
+
+@pytest.mark.parametrize("prec", ["mixed_df32", "mixed", "fp64"])
+def test_gemm_wait_expiry_reported_by_the_same_call(cuda, prec):
+    """Every pipeline wait of the tensor-core GEMMs made to give up at once
+    (poll limit 0) on a non-blocking stream: the ETRS step that ran the
+    GEMMs returns QBG_ERR_TIMEOUT itself (the error word is read on the
+    caller's stream), each CTA drains its own copies and MMAs before it frees
+    its memory, and the plan is usable again afterwards."""
+    torch = _torch()
+    H, psi, occ = make("t12", prec)
+    p = dev(psi)
+    ref = torch.zeros_like(p)
+    H.hpsi(p, ref, occ)
+    s = torch.cuda.Stream()  # non-blocking with respect to the legacy stream
+    H.set_wait_polls(0)
+    with pytest.raises(Q.QbgError, match="timeout"):
+        H.etrs_step(p.clone(), occ, 0.05, stream=s)
+    with pytest.raises(Q.QbgError, match="timeout"):
+        H.hpsi(p, torch.zeros_like(p), occ, stream=s)
+    H.set_wait_polls(-1)
+    out = torch.zeros_like(p)
+    H.hpsi(p, out, occ, stream=s)
+    s.synchronize()
+    assert rel_err(out.cpu().numpy(), ref.cpu().numpy()) < 1e-14

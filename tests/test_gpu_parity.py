@@ -117,9 +117,10 @@ def test_fft_padded_leading_dimension(cuda):
     assert np.all(oh[:, b.ngw:] == 7.0)  # padding rows untouched
 
 
-@pytest.mark.parametrize("name", ["t12", "c1"])
-def test_hpsi_fp64_vs_oracle(cuda, name):
+@pytest.mark.parametrize("name,gemm", [("t12", "ozaki"), ("c1", "ozaki"), ("c1", "simt")])
+def test_hpsi_fp64_vs_oracle(cuda, name, gemm):
     cell, b, H, oft, oh, psi = setup(name)
+    H.set_fp64_gemm(gemm)
     occ = synth.occupations(cell)
     torch = _torch()
     out = torch.zeros_like(dev(psi))
@@ -145,6 +146,68 @@ def test_hpsi_216_atom_grid(cuda, prec, tol):
     H.hpsi(dev(psi), out, occ)
     ref, _ = oh.hpsi(psi.T, occ, nthreads=NT)
     assert rel_err(out.cpu().numpy(), ref.T) < tol
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("mixed_df32", 2e-6)])
+def test_hpsi_216_atom_grid_full_chunk(cuda, prec, tol):
+    """The 216-atom cell's 120^3 grid and basis with 40 states: one full
+    32-state transform chunk plus a last chunk of 8, the tensor-core GEMM1
+    split over K, and E_nl."""
+    cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=40)
+    occ = synth.occupations(cell)
+    torch = _torch()
+    out = torch.zeros_like(dev(psi))
+    enl = H.hpsi(dev(psi), out, occ, want_enl=True)
+    ref, enl_ref = oh.hpsi(psi.T, occ, nthreads=NT)
+    assert rel_err(out.cpu().numpy(), ref.T) < tol
+    assert abs(enl - enl_ref) <= tol * abs(enl_ref)
+
+
+@pytest.mark.parametrize("name", ["c1", "c1q"])
+def test_etrs_and_density_c1_grids_vs_oracle(cuda, name):
+    """One ETRS step and the density of the 8-atom cell on the 48^3 grid and
+    on the reference's own dense-grid rule for it (64^3), FP64, against the
+    oracle: psi(t+dt), the density of the predicted state built inside
+    update(), its electron count, and the density of psi(t+dt)."""
+    cell, b, H, oft, oh, psi = setup(name)
+    occ = synth.occupations(cell)
+    A = synth.kick()
+    torch = _torch()
+    p = dev(psi)
+    rho = torch.zeros(oft.n012, dtype=torch.float64, device=cuda)
+    nel = H.etrs_step(p, occ, 0.05, A_t=A, A_tdt=A, rho=rho, want_nel=True)
+    oh.set_A(A)
+    ref, rref, nref = oh.etrs_step(psi.T.copy(), occ, 0.05, A, A, want_rho=True, nthreads=NT)
+    assert rel_err(p.cpu().numpy(), ref.T) < 1e-10
+    assert rel_err(rho.cpu().numpy(), rref) < 1e-10
+    assert abs(nel - nref) < 1e-10 * nref
+    rho2 = torch.zeros_like(rho)
+    nel2 = H.update_density(p, occ, rho2)
+    rref2, nref2 = O.update_density(oft, ref, occ)
+    assert rel_err(rho2.cpu().numpy(), rref2) < 1e-10
+    assert abs(nel2 - nref2) < 1e-10 * nref2
+
+
+@pytest.mark.parametrize("name,kw,slices,tol", [("c1", {}, 7, 1e-13), ("c1", {}, 6, 1e-11),
+                                                ("t12b", {}, 7, 1e-13),
+                                                ("c2", dict(natoms=8, nst=40), 7, 1e-13)])
+def test_fp64_tensor_core_gemm_matches_fp64_fma_gemm(cuda, name, kw, slices, tol):
+    """The plain form's projector GEMMs on the tensor cores (Ozaki scheme:
+    7-bit integer slices, exact FP32 windows) against the same form's FP64
+    FMA GEMMs on the same inputs: H|psi> and E_nl agree to the rounding of
+    the slices (49 bits for 7 slices, 42 for 6)."""
+    cell, b, H, oft, oh, psi = setup(name, **kw)
+    occ = synth.occupations(cell)
+    torch = _torch()
+    p = dev(psi)
+    outs, enls = {}, {}
+    for mode in ("simt", "ozaki"):
+        H.set_fp64_gemm(mode, slices)
+        o = torch.zeros_like(p)
+        enls[mode] = H.hpsi(p, o, occ, want_enl=True)
+        outs[mode] = o.cpu().numpy()
+    assert rel_err(outs["ozaki"], outs["simt"]) < tol
+    assert abs(enls["ozaki"] - enls["simt"]) <= tol * abs(enls["simt"])
 
 
 def test_hpsi_pieces_local_only_and_no_states(cuda):

@@ -24,7 +24,10 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("L,ecut,grid,nb", [(12.0, 10.0, (32, 32, 32), 5),
-                                            (20.0, 10.0, (48, 48, 48), 24)])
+                                            (20.0, 10.0, (48, 48, 48), 24),
+                                            # 216-atom basis: one state per pass, three
+                                            # passes reusing the static array
+                                            (30.0, 25.0, (120, 120, 120), 3)])
 def test_noalloc_backward_matches_backward_twice(cuda, L, ecut, grid, nb):
     import torch
     b = Q.Basis(L, ecut)
