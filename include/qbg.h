@@ -173,6 +173,27 @@ qbg_status qbg_set_nonlocal(qbg_plan* plan, int nsp, const int* na,
                             const int* lmax, const double* rc,
                             const double* wt, const double* tau);
 
+/* Kleinman-Bylander projectors given as tables, for real pseudopotentials:
+ * the arrays NonLocalPotential::init and update_twnl build
+ * (NonLocalPotential.cc:76-259, 261-760) from Species::dvnlg (Species.cc:
+ * 1492) and the real harmonics.  All host arrays, species after species:
+ * na[nsp] atoms and npr[nsp] projectors per species; lproj[sum npr] the
+ * angular momentum (0..3) of projector ipr (NonLocalPotential::lproj);
+ * wt[sum npr] its KB weight in Hartree (NonLocalPotential::wt, i.e.
+ * Species::wsg); twnl[sum npr][ngw] its radial-angular factor on the basis
+ * (twnl[is][ig + ngw*ipr]), evaluated at |k+G-A| for the vector potential in
+ * force; tau[3*sum na] atom positions (bohr).  H then applies
+ * anl = twnl (-i)^l exp(-i(k+G-A).tau) exactly as NonLocalPotential::energy
+ * (:1962-2037).  The tables depend on A: after qbg_set_vector_potential the
+ * caller passes them again for the new A, as the reference re-runs
+ * update_twnl (EnergyFunctional.cc:2047-2055); the adjoint's derivative
+ * along A is not available with tables (QBG_ERR_UNSUPPORTED).  Replaces
+ * what qbg_set_nonlocal set. */
+qbg_status qbg_set_nonlocal_tables(qbg_plan* plan, int nsp, const int* na,
+                                   const int* npr, const int* lproj,
+                                   const double* wt, const double* twnl,
+                                   const double* tau);
+
 /* Velocity-gauge vector potential A (host double[3]); recomputes
  * |k+G-A|^2 (VectorPotential::get_kpgpa2, VectorPotential.h:84-95) and the
  * projector tables for k+G-A (EnergyFunctional::vector_potential_changed,

@@ -1,7 +1,10 @@
 #!/bin/sh
 # Build oracle/_ref/libqbref.so from the reference's own serial sources
 # (Basis.cc, FourierTransform.cc with its internal FFT_NOLIB transform,
-# UnitCell.cc, functionals/LDAFunctional.cc), compiled in place from the read-only reference tree, plus the
+# UnitCell.cc, functionals/LDAFunctional.cc, the pseudopotential Species with
+# its reader, radial sine transform, spherical integration and splines, and
+# the vendored header-only XML parser), compiled in place from the read-only
+# reference tree, plus the
 # one-process Context stub and the C shim in this folder.  The reference's
 # build system is not used.  Test infrastructure only.
 #
@@ -23,8 +26,12 @@ fi
 mkdir -p "$OUT"
 g++ -O2 -fPIC -shared -std=c++11 -w \
   -I"$HERE/ref_stub" -I"$REF/src" -I"$REF/src/qball" -I"$REF/src/functionals" \
+  -I"$REF/external_libs/rapidxml" -DSHARE_DIR="\"$REF/share\"" \
   "$REF/src/qball/Basis.cc" "$REF/src/qball/FourierTransform.cc" \
   "$REF/src/qball/UnitCell.cc" "$REF/src/functionals/LDAFunctional.cc" \
+  "$REF/src/qball/Species.cc" "$REF/src/qball/SpeciesReader.cc" \
+  "$REF/src/qball/sinft.cc" "$REF/src/qball/SphericalIntegration.cc" \
+  "$REF/src/pseudo/spline.cc" \
   "$HERE/ref_stub/ref_context_stub.cc" "$HERE/ref_shim.cc" \
   -o "$OUT/libqbref.so"
 echo "built $OUT/libqbref.so"

@@ -60,6 +60,7 @@ def lib():
         L.qbo_ham_set_A.argtypes = [_P, _P]
         L.qbo_ham_nproj.argtypes = [_P]
         L.qbo_ham_projector.argtypes = [_P, _I, _P, _P, _P, _P]
+        L.qbo_ham_set_species_tables.argtypes = [_P, _I, _I, _P, _P, _P]
         L.qbo_hpsi.argtypes = [_P, _P, _I, _I, _P, _P, _I]
         L.qbo_hpsi.restype = _D
         L.qbo_nl_apply.argtypes = [_P, _P, _I, _I, _P, _P, _I]
@@ -104,7 +105,46 @@ def ref():
         R.qbref_ft_backward.argtypes = [_P, _P, _P]
         R.qbref_ft_forward.argtypes = [_P, _P, _P]
         R.qbref_lda.argtypes = [_I, _P, _P, _P]
+        R.qbref_species_load.argtypes = [ctypes.c_char_p, _D]
+        R.qbref_species_load.restype = _P
+        R.qbref_species_destroy.argtypes = [_P]
+        R.qbref_species_info.argtypes = [_P, _P]
+        R.qbref_species_wsg.argtypes = [_P, _I, _I]
+        R.qbref_species_wsg.restype = _D
+        R.qbref_species_vnlg.argtypes = [_P, _I, _I, _I, _P, _P]
     return _ref
+
+
+def ref_species_load(path, rcps=1.0):
+    """A pseudopotential read and initialised by the reference's own Species
+    code (handle; ref_species_destroy frees it)."""
+    h = ref().qbref_species_load(path.encode(), float(rcps))
+    if not h:
+        raise OSError(f"reference Species could not read {path}")
+    return h
+
+
+def ref_species_destroy(h):
+    ref().qbref_species_destroy(h)
+
+
+def ref_species_info(h):
+    """[lmax, llocal, nchannels, nlm, zval, nquad, ultrasoft, 0]"""
+    info = np.zeros(8, np.int32)
+    ref().qbref_species_info(h, _ptr(info))
+    return info
+
+
+def ref_species_wsg(h, l, ic):
+    return float(ref().qbref_species_wsg(h, int(l), int(ic)))
+
+
+def ref_species_vnlg(h, l, ic, g):
+    """Species::dvnlg(l, ic, g) values for the |G| values g."""
+    g = np.ascontiguousarray(g, np.float64)
+    v = np.zeros_like(g)
+    ref().qbref_species_vnlg(h, int(l), int(ic), g.size, _ptr(g), _ptr(v))
+    return v
 
 
 def ref_lda(rho):
@@ -223,16 +263,22 @@ class Ham:
     """Restated Hamiltonian (kinetic + local + KB nonlocal) and ETRS step."""
 
     def __init__(self, ft, v_r, species):
-        """species: list of dicts {tau: (na,3), lmax, rc, wt: [w0,w1,w2]}."""
+        """species: list of dicts {tau: (na,3), lmax, rc, wt: [w0,w1,w2]} (the
+        synthetic radial form) or {tau, twnl: (npr, ngw), lproj: (npr,), wt:
+        (npr,)} (projector tables as NonLocalPotential::update_twnl builds
+        them, evaluated at |k+G-A| for the A in force)."""
         self.ft = ft
         b = ft.basis
         self.v_r = np.ascontiguousarray(v_r, dtype=np.float64)
         nsp = len(species)
+        tables = [("twnl" in s) for s in species]
         self.na = np.array([len(s["tau"]) for s in species], np.int32)
-        self.lmax = np.array([s["lmax"] for s in species], np.int32)
-        self.rc = np.array([s["rc"] for s in species], np.float64)
+        self.lmax = np.array([-1 if t else s["lmax"] for s, t in zip(species, tables)], np.int32)
+        self.rc = np.array([s.get("rc", 1.0) for s in species], np.float64)
         self.wt = np.zeros(3 * max(nsp, 1))
         for i, s in enumerate(species):
+            if tables[i]:
+                continue
             w = list(s["wt"]) + [0.0] * 3
             self.wt[3 * i:3 * i + 3] = w[:3]
         self.tau = np.ascontiguousarray(
@@ -241,6 +287,12 @@ class Ham:
         self.h = lib().qbo_ham_create(ft.h, b.ngw, _ptr(b.kpgx), b.omega, _ptr(self.v_r),
                                       nsp, _ptr(self.na), _ptr(self.lmax), _ptr(self.rc),
                                       _ptr(self.wt), _ptr(self.tau))
+        for i, s in enumerate(species):
+            if tables[i]:
+                tw = np.ascontiguousarray(s["twnl"], np.float64)
+                lp = np.ascontiguousarray(s["lproj"], np.int32)
+                w = np.ascontiguousarray(s["wt"], np.float64)
+                lib().qbo_ham_set_species_tables(self.h, i, len(lp), _ptr(lp), _ptr(w), _ptr(tw))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -399,9 +399,11 @@ void qbo_ft_forward(const qbo_ft* ft, double* f, double* c) {
 typedef struct {
   int na, lmax, npr;
   double rc, wt[3];
-  double* tau; /* 3*na */
-  int lproj[9];
-  double* twnl; /* npr*ngw after set_A */
+  double* tau;   /* 3*na */
+  int* lproj;    /* npr: l of projector ipr (NonLocalPotential::lproj) */
+  double* wtp;   /* npr: weight of projector ipr (NonLocalPotential::wt) */
+  double* twnl;  /* npr*ngw: after set_A (synthetic) or as given (tables) */
+  int tables;    /* twnl given by the caller: set_A does not rebuild it */
 } qbo_species;
 
 struct qbo_ham {
@@ -443,9 +445,14 @@ qbo_ham* qbo_ham_create(const qbo_ft* ft, int ngw, const double* kpgx,
     p->npr = 0;
     /* NonLocalPotential::init (NonLocalPotential.cc:205-250): projectors
      * ordered by l, then m; one KB channel per l */
+    p->lproj = (int*)calloc(9, sizeof(int));
+    p->wtp = (double*)calloc(9, sizeof(double));
     for (int l = 0; l <= p->lmax; ++l) {
       p->wt[l] = wt[3 * s + l];
-      for (int m = 0; m < 2 * l + 1; ++m) p->lproj[p->npr++] = l;
+      for (int m = 0; m < 2 * l + 1; ++m) {
+        p->wtp[p->npr] = p->wt[l];
+        p->lproj[p->npr++] = l;
+      }
     }
     p->tau = (double*)malloc(sizeof(double) * 3 * (size_t)(p->na > 0 ? p->na : 1));
     memcpy(p->tau, tau + 3 * atom0, sizeof(double) * 3 * (size_t)p->na);
@@ -462,6 +469,8 @@ void qbo_ham_destroy(qbo_ham* h) {
   for (int s = 0; s < h->nsp; ++s) {
     free(h->sp[s].tau);
     free(h->sp[s].twnl);
+    free(h->sp[s].lproj);
+    free(h->sp[s].wtp);
   }
   free(h->sp);
   free(h->kpgx);
@@ -512,6 +521,7 @@ void qbo_ham_set_A(qbo_ham* h, const double* A) {
   const double s54pi = sqrt(5.0 / fpi), s3 = sqrt(3.0);
   for (int s = 0; s < h->nsp; ++s) {
     qbo_species* p = &h->sp[s];
+    if (p->tables) continue;
     for (int ig = 0; ig < ng; ++ig) {
       const double kpg2 = h->kpg2A[ig];
       const double tg = sqrt(kpg2);
@@ -564,7 +574,7 @@ void qbo_ham_projector(const qbo_ham* h, int p, double* twnl, int* l,
       const int ipr = p / sp->na, ia = p % sp->na;
       if (twnl) memcpy(twnl, sp->twnl + (size_t)h->ngw * ipr, sizeof(double) * (size_t)h->ngw);
       if (l) *l = sp->lproj[ipr];
-      if (wt) *wt = sp->wt[sp->lproj[ipr]];
+      if (wt) *wt = sp->wtp[ipr];
       if (tau3) {
         tau3[0] = sp->tau[3 * ia];
         tau3[1] = sp->tau[3 * ia + 1];
@@ -574,6 +584,27 @@ void qbo_ham_projector(const qbo_ham* h, int p, double* twnl, int* l,
     }
     p -= n;
   }
+}
+
+/* Projector tables of species s given by the caller, as NonLocalPotential::
+ * init / update_twnl hold them (NonLocalPotential.cc:205-250, 261-760):
+ * npr projectors with l = lproj[ipr] (0..3), weights wt[ipr] (Species::wsg),
+ * twnl[ipr*ngw + ig] evaluated at |k+G-A| for the A in force.  set_A then
+ * only moves the structure-factor phases. */
+void qbo_ham_set_species_tables(qbo_ham* h, int s, int npr, const int* lproj,
+                                const double* wt, const double* twnl) {
+  qbo_species* p = &h->sp[s];
+  free(p->lproj);
+  free(p->wtp);
+  free(p->twnl);
+  p->npr = npr;
+  p->lproj = (int*)calloc((size_t)(npr > 0 ? npr : 1), sizeof(int));
+  p->wtp = (double*)calloc((size_t)(npr > 0 ? npr : 1), sizeof(double));
+  p->twnl = (double*)calloc((size_t)npr * h->ngw + 1, sizeof(double));
+  memcpy(p->lproj, lproj, sizeof(int) * (size_t)npr);
+  memcpy(p->wtp, wt, sizeof(double) * (size_t)npr);
+  memcpy(p->twnl, twnl, sizeof(double) * (size_t)npr * h->ngw);
+  p->tables = 1;
 }
 
 /* anl column (NonLocalPotential.cc:1962-2037): twnl * (-i)^l * exp(-i(k+G-A).tau) */
@@ -597,9 +628,12 @@ static void qbo_anl_column(const qbo_ham* h, const qbo_species* sp, int ipr,
     } else if (l == 1) {
       re = t[ig] * s;
       im = -t[ig] * c;
-    } else {
+    } else if (l == 2) {
       re = -t[ig] * c;
       im = -t[ig] * s;
+    } else {
+      re = -t[ig] * s;
+      im = t[ig] * c;
     }
     a[2 * ig] = re;
     a[2 * ig + 1] = im;
@@ -655,7 +689,7 @@ double qbo_nl_apply(const qbo_ham* h, const double* c, int ld, int nst,
       }
       /* Enl and D scaling (NonLocalPotential.cc:2124-2146) */
       for (int ipr = 0; ipr < sp->npr; ++ipr) {
-        const double fac = sp->wt[sp->lproj[ipr]] * omega_inv;
+        const double fac = sp->wtp[ipr] * omega_inv;
         for (int n = 0; n < nst; ++n) {
           const double facn = fac * (occ ? occ[n] : 0.0);
           for (int ia = 0; ia < nblk; ++ia) {

@@ -63,6 +63,8 @@ void qbo_ham_destroy(qbo_ham* h);
 void qbo_ham_set_A(qbo_ham* h, const double* A);
 int qbo_ham_nproj(const qbo_ham* h);
 /* twnl for projector p (after set_A), ngw doubles; lproj / wt per projector */
+void qbo_ham_set_species_tables(qbo_ham* h, int s, int npr, const int* lproj,
+                                const double* wt, const double* twnl);
 void qbo_ham_projector(const qbo_ham* h, int p, double* twnl, int* l,
                        double* wt, double* tau3);
 /* cp = H c for nst states (EnergyFunctional.cc:1142-1152,1500,1639-1701);

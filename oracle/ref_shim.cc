@@ -8,6 +8,8 @@
 #include "FourierTransform.h"
 #include "UnitCell.h"
 #include "LDAFunctional.h"
+#include "Species.h"
+#include "SpeciesReader.h"
 #include <complex>
 #include <vector>
 
@@ -98,6 +100,67 @@ void qbref_lda(int n, const double* rho, double* exc, double* vxc) {
   for (int i = 0; i < n; ++i) {
     exc[i] = f.exc[i];
     vxc[i] = f.vxc1[i];
+  }
+}
+
+// ---- Species (Species.cc, SpeciesReader.cc): a pseudopotential read from
+// its file by the reference's own reader and initialised by
+// Species::initialize (radial Bessel transforms, KB weights, splines).
+namespace {
+struct RefSpecies {
+  Context ctxt;
+  Species* sp;
+};
+}
+
+// path: species file (QSO XML, UPF, ...); rcps: Gaussian pseudo-charge
+// radius.  NULL when reading or initialising fails.
+void* qbref_species_load(const char* path, double rcps) {
+  RefSpecies* r = new RefSpecies;
+  r->sp = new Species(r->ctxt, "sp");
+  try {
+    SpeciesReader rd(r->ctxt);
+    rd.readSpecies(*r->sp, path);
+    if (!r->sp->initialize(rcps)) throw 1;
+  } catch (...) {
+    delete r->sp;
+    delete r;
+    return nullptr;
+  }
+  return r;
+}
+
+void qbref_species_destroy(void* h) {
+  RefSpecies* r = static_cast<RefSpecies*>(h);
+  delete r->sp;
+  delete r;
+}
+
+// info[0]=lmax [1]=llocal [2]=nchannels [3]=nlm [4]=zval [5]=nquad
+// [6]=ultrasoft [7]=oncv
+void qbref_species_info(void* h, int* info) {
+  Species& s = *static_cast<RefSpecies*>(h)->sp;
+  info[0] = s.lmax();
+  info[1] = s.llocal();
+  info[2] = s.nchannels();
+  info[3] = s.nlm();
+  info[4] = s.zval();
+  info[5] = s.nquad();
+  info[6] = s.ultrasoft() ? 1 : 0;
+  info[7] = 0;
+}
+
+// Kleinman-Bylander weight wsg(l, ic) = 1 / <phi|dV|phi>
+double qbref_species_wsg(void* h, int l, int ic) {
+  return static_cast<RefSpecies*>(h)->sp->wsg(l, ic);
+}
+
+// v[i] = the radial projector of (l, ic) at |G| = g[i] (Species::dvnlg)
+void qbref_species_vnlg(void* h, int l, int ic, int n, const double* g, double* v) {
+  Species& s = *static_cast<RefSpecies*>(h)->sp;
+  for (int i = 0; i < n; ++i) {
+    double dv;
+    s.dvnlg(l, ic, g[i], v[i], dv);
   }
 }
 

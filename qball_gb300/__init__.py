@@ -61,6 +61,7 @@ ABI = {
     "qbg_set_vlocal": [_P, _P],
     "qbg_get_vlocal": [_P, _P],
     "qbg_set_nonlocal": [_P, _I, _P, _P, _P, _P, _P],
+    "qbg_set_nonlocal_tables": [_P, _I, _P, _P, _P, _P, _P, _P],
     "qbg_set_vector_potential": [_P, _P],
     "qbg_hpsi": [_P, _P, _I, _P, _I, _P, _P, _P],
     "qbg_density": [_P, _P, _I, _I, _P, _D, _P, _P, _P],
@@ -286,7 +287,12 @@ class Hamiltonian(FourierTransform):
         return v
 
     def set_nonlocal(self, species):
-        """species: list of {tau: (na,3), lmax, rc, wt: [w_s, w_p, w_d]}."""
+        """species: list of {tau: (na,3), lmax, rc, wt: [w_s, w_p, w_d]} (the
+        synthetic radial form), or of {tau, twnl: (npr, ngw), lproj: (npr,),
+        wt: (npr,)} (projector tables of real pseudopotentials as
+        NonLocalPotential::update_twnl builds them, for the A in force)."""
+        if species and all("twnl" in s for s in species):
+            return self.set_nonlocal_tables(species)
         nsp = len(species)
         na = np.array([len(s["tau"]) for s in species], np.int32)
         lmax = np.array([s["lmax"] for s in species], np.int32)
@@ -300,6 +306,25 @@ class Hamiltonian(FourierTransform):
                if nsp else np.zeros(3))
         _check(lib().qbg_set_nonlocal(self.h, nsp, _np_ptr(na), _np_ptr(lmax), _np_ptr(rc),
                                       _np_ptr(wt), _np_ptr(tau)), "qbg_set_nonlocal")
+
+    def set_nonlocal_tables(self, species):
+        """Projector tables (qbg_set_nonlocal_tables): per species tau (na,3),
+        twnl (npr, ngw) at |k+G-A|, lproj (npr,), wt (npr,) in Hartree."""
+        nsp = len(species)
+        na = np.array([len(s["tau"]) for s in species], np.int32)
+        npr = np.array([len(s["lproj"]) for s in species], np.int32)
+        lproj = np.ascontiguousarray(np.concatenate([np.asarray(s["lproj"], np.int32)
+                                                     for s in species]), np.int32)
+        wt = np.ascontiguousarray(np.concatenate([np.asarray(s["wt"], np.float64)
+                                                  for s in species]), np.float64)
+        twnl = np.ascontiguousarray(np.concatenate([np.asarray(s["twnl"], np.float64)
+                                                    .reshape(-1, self.basis.ngw)
+                                                    for s in species]), np.float64)
+        tau = np.ascontiguousarray(np.concatenate([np.asarray(s["tau"], np.float64).reshape(-1)
+                                                   for s in species]), np.float64)
+        _check(lib().qbg_set_nonlocal_tables(self.h, nsp, _np_ptr(na), _np_ptr(npr),
+                                             _np_ptr(lproj), _np_ptr(wt), _np_ptr(twnl),
+                                             _np_ptr(tau)), "qbg_set_nonlocal_tables")
 
     # ---- Hartree + xc (EnergyFunctional::update_vhxc)
     def set_density_basis(self, vbasis):

@@ -21,11 +21,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 
 
-def run_form(precision, cell, basis, psi0, occ, A, dt, steps, chunk=0, hxc=True):
+# form label -> (precision form, projector GEMMs of the plain FP64 form)
+FORMS = {"fp64": ("fp64", "ozaki"), "fp64_simt": ("fp64", "simt")}
+
+
+def run_form(label, cell, basis, psi0, occ, A, dt, steps, chunk=0, hxc=True):
     import torch
     import qball_gb300 as Q
     from qball_gb300 import synth
+    precision, gemm = FORMS.get(label, (label, None))
     H = Q.Hamiltonian(basis, *cell.grid, precision=precision)
+    if gemm:
+        H.set_fp64_gemm(gemm)
     if chunk:
         H.set_chunk(chunk)
     H.set_vlocal(synth.vlocal(cell))
@@ -66,6 +73,10 @@ def main():
     ap.add_argument("--ref", default="", help="npz of an earlier run: reuse its fp64 d(t)")
     ap.add_argument("--hxc", default="on", choices=["on", "off"],
                     help="self-consistent Hartree + LDA potential (as bench.py)")
+    ap.add_argument("--simt-steps", type=int, default=0,
+                    help="also run the FP64 form with FP64-FMA projector GEMMs for this many "
+                         "steps and compare it with the tensor-core FP64 form over them")
+    ap.add_argument("--json", default="", help="write the report to this file")
     args = ap.parse_args()
     kw = {"nst": args.nst} if args.nst else {}
     cell = synth.make_cell(args.config, **kw)
@@ -99,7 +110,24 @@ def main():
                                  "psi_rel_err_final": pd, "seconds": r.get("seconds"),
                                  "steps_per_s": (args.steps / r["seconds"]) if r.get("seconds")
                                  else None}
+    if args.simt_steps > 0:
+        # the FP64 trajectory itself against the FP64-FMA GEMMs over its first steps
+        n = args.simt_steps
+        r = run_form("fp64_simt", cell, basis, psi0, occ, A, args.dt, n, hxc=args.hxc == "on")
+        r64 = run_form("fp64", cell, basis, psi0, occ, A, args.dt, n, hxc=args.hxc == "on")
+        dn = r["d"][:n + 1]
+        dz = np.abs(dn[:, 2]).max()
+        report["fp64_vs_fp64_simt"] = {
+            "steps": n,
+            "dipole_rel_err_z": float(np.abs(r64["d"][:, 2] - dn[:, 2]).max() / dz),
+            "current_max_abs_diff": float(np.abs(r64["J"] - r["J"]).max()),
+            "psi_rel_err_final": float(((r64["psi"] - r["psi"]).abs().pow(2).sum().sqrt()
+                                        / r["psi"].abs().pow(2).sum().sqrt()).item()),
+            "seconds_per_step_simt": r["seconds"] / n}
     print(json.dumps(report), flush=True)
+    if args.json:
+        with open(args.json, "w") as f:
+            json.dump(report, f, indent=1)
     if args.out:
         np.savez(args.out, **{f"{k}_d": v["d"] for k, v in res.items()},
                  **{f"{k}_J": v["J"] for k, v in res.items()})

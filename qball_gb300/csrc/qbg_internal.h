@@ -98,6 +98,11 @@ struct qbg_plan {
   int nsp = 0;
   std::vector<int> sp_na, sp_lmax;
   std::vector<double> sp_rc, sp_wt, sp_tau;
+  bool nl_tables = false;      // projector tables given by the caller
+  std::vector<int> sp_npr, sp_lproj;  // per species / per table row
+  std::vector<double> sp_wtp;  // per table row: KB weight
+  double* d_twnl = nullptr;    // [rows][ngw] the caller's twnl tables
+  size_t twnl_bytes = 0;
   int* d_plist = nullptr;      // [nproj] packed (species, ipr, atom) -> int4-like
   double* d_ptau = nullptr;    // [3*nproj]
   double* d_pwt = nullptr;     // [nproj] wt/omega

@@ -18,19 +18,25 @@
 
 namespace qbg {
 
-// projector descriptor: l, m index within l, species radius, weight/omega
+// projector descriptor: l, m index within l, species radius, weight/omega;
+// row >= 0: the radial-angular factor is row `row` of the caller's tables
+// (qbg_set_nonlocal_tables), else the synthetic radial form
 struct ProjDesc {
   int l, m;
   double rc, wt;
   double tau[3];
+  int row;
 };
 
 // update_twnl (NonLocalPotential.cc:306-760) for the synthetic radial form,
 // evaluated at k+G-A, times (-i)^l exp(-i (k+G-A).tau)  (:1962-2037).
+// With caller tables (pd[p].row >= 0) the factor twnl[row][g] is taken as
+// given, for l = 0..3.
 template <bool MIXED>
 __global__ void k_anl(const double* __restrict__ kpgx, const double* __restrict__ kpg2A,
                       int ngw, double A0, double A1, double A2,
                       const ProjDesc* __restrict__ pd, int nproj,
+                      const double* __restrict__ twnl,
                       double2* __restrict__ anl, float2* __restrict__ anl32) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   const int p = blockIdx.y;
@@ -43,7 +49,9 @@ __global__ void k_anl(const double* __restrict__ kpgx, const double* __restrict_
   const double e = exp(-0.5 * tg * tg * d.rc * d.rc);
   const double pi = 3.14159265358979323846, fpi = 4.0 * pi;
   double t;
-  if (d.l == 0) {
+  if (d.row >= 0) {
+    t = twnl[(size_t)d.row * ngw + g];
+  } else if (d.l == 0) {
     t = sqrt(1.0 / fpi) * e;
   } else if (d.l == 1) {
     const double s34pi = sqrt(3.0 / fpi);
@@ -75,9 +83,12 @@ __global__ void k_anl(const double* __restrict__ kpgx, const double* __restrict_
   } else if (d.l == 1) {
     re = t * s;
     im = -t * c;
-  } else {
+  } else if (d.l == 2) {
     re = -t * c;
     im = -t * s;
+  } else {
+    re = -t * s;
+    im = t * c;
   }
   const size_t o = (size_t)p * ngw + g;
   anl[o] = make_double2(re, im);
@@ -116,6 +127,31 @@ static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector
   for (int s = 0; s < p->nsp; ++s) namax = std::max(namax, p->sp_na[s]);
   const int nbs = std::max(1, std::min(namax, 128));
   int atom0 = 0;
+  if (p->nl_tables) {
+    // caller tables: npr[s] projectors of species s with l = lproj, weight wt
+    int row0 = 0;
+    for (int s = 0; s < p->nsp; ++s) {
+      const int na = p->sp_na[s], npr = p->sp_npr[s];
+      for (int b0 = 0; b0 < na; b0 += nbs) {
+        const int b1 = std::min(na, b0 + nbs);
+        for (int ipr = 0; ipr < npr; ++ipr)
+          for (int ia = b0; ia < b1; ++ia) {
+            ProjDesc d;
+            d.l = p->sp_lproj[row0 + ipr];
+            d.m = 0;
+            d.rc = 0.0;
+            d.wt = p->sp_wtp[row0 + ipr] / p->omega;
+            for (int j = 0; j < 3; ++j) d.tau[j] = p->sp_tau[3 * (size_t)(atom0 + ia) + j];
+            d.row = row0 + ipr;
+            pd.push_back(d);
+            wt.push_back(d.wt);
+          }
+      }
+      atom0 += na;
+      row0 += npr;
+    }
+    return;
+  }
   for (int s = 0; s < p->nsp; ++s) {
     const int na = p->sp_na[s], lmax = p->sp_lmax[s];
     for (int b0 = 0; b0 < na; b0 += nbs) {
@@ -129,6 +165,7 @@ static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector
             d.rc = p->sp_rc[s];
             d.wt = p->sp_wt[3 * s + l] / p->omega;
             for (int j = 0; j < 3; ++j) d.tau[j] = p->sp_tau[3 * (size_t)(atom0 + ia) + j];
+            d.row = -1;
             pd.push_back(d);
             wt.push_back(d.wt);
           }
@@ -181,7 +218,8 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
   QBG_CUDA(cudaMemcpy(p->d_pwt, wt.data(), sizeof(double) * P, cudaMemcpyHostToDevice));
   dim3 grid((p->ngw + 255) / 256, P);
   k_anl<false><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
-                                     (const ProjDesc*)p->d_pdesc, P, p->d_anl, nullptr);
+                                     (const ProjDesc*)p->d_pdesc, P, p->d_twnl, p->d_anl,
+                                     nullptr);
   p->launches++;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -463,6 +501,11 @@ __global__ void k_anl_da(const double* __restrict__ kpgx, const double* __restri
 
 qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_t st) {
   if (p->nproj == 0 || p->ngw == 0) return QBG_OK;
+  if (p->nl_tables) {
+    set_error("projector derivative along A: not available for caller projector tables "
+              "(qbg_set_nonlocal_tables carries no radial derivative)");
+    return QBG_ERR_UNSUPPORTED;
+  }
   if (!p->nl_ready || !p->d_pdesc) {
     set_error("projector derivative: the projector table is not built");
     return QBG_ERR_STATE;

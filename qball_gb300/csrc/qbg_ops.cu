@@ -264,11 +264,58 @@ qbg_status qbg_set_nonlocal(qbg_plan* p, int nsp, const int* na, const int* lmax
     return QBG_ERR_INVALID;
   }
   p->nsp = nsp;
+  p->nl_tables = false;
   p->sp_na.assign(na, na + nsp);
   p->sp_lmax.assign(lmax, lmax + nsp);
   p->sp_rc.assign(rc, rc + nsp);
   p->sp_wt.assign(wt, wt + 3 * nsp);
   p->sp_tau.assign(tau, tau + 3 * (size_t)ntot);
+  p->nl_ready = false;
+  return nl_build(p, 0);
+}
+
+qbg_status qbg_set_nonlocal_tables(qbg_plan* p, int nsp, const int* na, const int* npr,
+                                   const int* lproj, const double* wt, const double* twnl,
+                                   const double* tau) {
+  if (!p || nsp < 0 || (nsp > 0 && (!na || !npr))) {
+    set_error("qbg_set_nonlocal_tables: invalid argument");
+    return QBG_ERR_INVALID;
+  }
+  size_t rows = 0, ntot = 0;
+  for (int s = 0; s < nsp; ++s) {
+    if (na[s] < 0 || npr[s] < 0) {
+      set_error("qbg_set_nonlocal_tables: species %d has na=%d npr=%d", s, na[s], npr[s]);
+      return QBG_ERR_INVALID;
+    }
+    rows += npr[s];
+    ntot += na[s];
+  }
+  if ((rows > 0 && (!lproj || !wt || !twnl)) || (ntot > 0 && !tau)) {
+    set_error("qbg_set_nonlocal_tables: null table");
+    return QBG_ERR_INVALID;
+  }
+  for (size_t r = 0; r < rows; ++r)
+    if (lproj[r] < 0 || lproj[r] > 3) {
+      set_error("qbg_set_nonlocal_tables: lproj[%zu] = %d (must be 0..3)", r, lproj[r]);
+      return QBG_ERR_INVALID;
+    }
+  // kernels of any stream may still read the old tables
+  QBG_CUDA(cudaDeviceSynchronize());
+  const size_t bytes = sizeof(double) * rows * (size_t)p->ngw;
+  if (bytes > 0) {
+    QBG_TRY(ensure((void**)&p->d_twnl, &p->twnl_bytes, bytes));
+    QBG_CUDA(cudaMemcpy(p->d_twnl, twnl, bytes, cudaMemcpyHostToDevice));
+  }
+  p->nsp = nsp;
+  p->nl_tables = true;
+  p->sp_na.assign(na, na + nsp);
+  p->sp_npr.assign(npr, npr + nsp);
+  p->sp_lproj.assign(lproj, lproj + rows);
+  p->sp_wtp.assign(wt, wt + rows);
+  p->sp_tau.assign(tau, tau + 3 * ntot);
+  p->sp_lmax.assign(nsp, -1);
+  p->sp_rc.assign(nsp, 0.0);
+  p->sp_wt.assign(3 * (size_t)nsp, 0.0);
   p->nl_ready = false;
   return nl_build(p, 0);
 }

@@ -56,7 +56,7 @@ constexpr int OZ_SMAX = 7;                         // most slices per operand
 constexpr int OZ_BLK = 4096;                       // one 128 x 16 FP16 block, bytes
 constexpr int OZ_SLOT = 2 * OZ_SMAX * OZ_BLK;      // A slices then B slices: 56 KB
 constexpr int OZ_STAGES = 4;
-constexpr int OZ_NBUF = 4;                         // tensor-memory blocks of 128 columns
+constexpr int OZ_NBUF = 3;                         // accumulators of 128 columns
 constexpr int OZ_THREADS = 576;                    // producer, MMA issuer, 16 epilogue warps
 constexpr int OZ_EPI = 512;
 constexpr int OZ_ECOLS = 32;
@@ -319,12 +319,12 @@ __device__ __forceinline__ bool oz_produce(const OzArgs& a, const OzCta& c, int 
 }
 
 // MMA issuer, one group: windows of g::win K steps; at a window's start the
-// accumulators it takes (bc, bc+1, .. mod 4) must have been read by the
+// accumulators it takes (blocks 0 .. nd-1) must have been read by the
 // epilogue; at its end each is committed to its accfull barrier.  used/par:
-// per tensor-memory block, used at least once / parity of its use count.
+// per accumulator, used at least once / parity of its use count.
 template <int G>
 __device__ __forceinline__ bool oz_mma(const OzArgs& a, const OzCta& c, uint32_t idesc, int nks,
-                                       int& q, int& bc, uint32_t& used, uint32_t& par) {
+                                       int& q, uint32_t& used, uint32_t& par) {
   using g = OzG<G>;
   for (int w0 = 0; w0 < nks; w0 += g::win) {
     const int w1 = min(nks, w0 + g::win);
@@ -332,7 +332,7 @@ __device__ __forceinline__ bool oz_mma(const OzArgs& a, const OzCta& c, uint32_t
     uint32_t tb[3];
 #pragma unroll
     for (int k = 0; k < g::nd; ++k) {
-      bb[k] = (bc + k) & (OZ_NBUF - 1);
+      bb[k] = k;
       tb[k] = c.tbase + (uint32_t)(bb[k] * 128);
       if ((used >> bb[k]) & 1) {
         if (!mbar_wait(&c.accempty[bb[k]], ((par >> bb[k]) & 1) ^ 1, a.status, a.polls))
@@ -362,46 +362,51 @@ __device__ __forceinline__ bool oz_mma(const OzArgs& a, const OzCta& c, uint32_t
       used |= 1u << bb[k];
       par ^= 1u << bb[k];
     }
-    bc += g::nd;
   }
   return true;
 }
 
 // Epilogue, one group: fold each closed accumulator (an exact integer sum
-// times 2^(-7 d)) into the compensated (hi, lo) pairs.
+// times 2^(-7 d)) into the compensated pair (hi, lo): hi in registers, lo in
+// the fourth tensor-memory block (columns 384-511).  The accumulator is
+// released as soon as it is in registers.
 template <int G>
 __device__ __forceinline__ bool oz_fold(const OzArgs& a, const OzCta& c, uint32_t taddr, int nks,
-                                        int& bc, uint32_t& par, float* hi, float* lo) {
+                                        uint32_t& par, float* hi) {
   using g = OzG<G>;
   for (int w0 = 0; w0 < nks; w0 += g::win) {
 #pragma unroll
     for (int k = 0; k < g::nd; ++k) {
-      const int b = (bc + k) & (OZ_NBUF - 1);
-      if (!mbar_wait(&c.accfull[b], (par >> b) & 1, a.status, a.polls)) return false;
+      if (!mbar_wait(&c.accfull[k], (par >> k) & 1, a.status, a.polls)) return false;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       // 2^(-7 d) as an FP32 bit pattern (d <= 8: exponent >= -56)
       const float sc = __uint_as_float((uint32_t)(127 - 7 * g::diag(k)) << 23);
+      uint32_t v[OZ_ECOLS];
+      tmem_ld16(taddr + k * 128, v);
+      tmem_ld16(taddr + k * 128 + 16, v + 16);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(&c.accempty[k]);
+      par ^= 1u << k;
 #pragma unroll
       for (int h = 0; h < OZ_ECOLS; h += 16) {
-        uint32_t v[16];
-        tmem_ld16(taddr + b * 128 + h, v);
+        uint32_t l[16];
+        tmem_ld16(taddr + 3 * 128 + h, l);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-          const float x = __uint_as_float(v[j]) * sc;
+          const float x = __uint_as_float(v[h + j]) * sc;
           const float y = hi[h + j];
           const float s = y + x;
           const float bbv = s - y;
           const float e = (y - (s - bbv)) + (x - bbv);
           hi[h + j] = s;
-          lo[h + j] += e;
+          l[j] = __float_as_uint(__uint_as_float(l[j]) + e);
         }
+        tmem_st16(taddr + 3 * 128 + h, l);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(&c.accempty[b]);
-      par ^= 1u << b;
     }
-    bc += g::nd;
   }
   return true;
 }
@@ -414,7 +419,7 @@ __device__ __forceinline__ double oz_scale2(double x, int e) {
 }
 
 template <int MODE>
-__global__ void __maxnreg__(112) k_oz_gemm(OzArgs args) {
+__global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs args) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   OzCta c;
   c.smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -475,11 +480,11 @@ __global__ void __maxnreg__(112) k_oz_gemm(OzArgs args) {
     } else if (warp == 1 && lane == 0) {
       // ---------------- MMA issuer
       const uint32_t idesc = idesc_f16_f32(OZ_M, OZ_N);
-      int q = 0, bc = 0;
+      int q = 0;
       uint32_t used = 0, par = 0;
-      const bool ok = oz_mma<0>(args, c, idesc, nks, q, bc, used, par) &&
-                      oz_mma<1>(args, c, idesc, nks, q, bc, used, par) &&
-                      (!g3 || oz_mma<2>(args, c, idesc, nks, q, bc, used, par));
+      const bool ok = oz_mma<0>(args, c, idesc, nks, q, used, par) &&
+                      oz_mma<1>(args, c, idesc, nks, q, used, par) &&
+                      (!g3 || oz_mma<2>(args, c, idesc, nks, q, used, par));
       if (!ok) {
         *c.abort_flag = 1;
         atomicExch(args.status, 1);
@@ -496,17 +501,21 @@ __global__ void __maxnreg__(112) k_oz_gemm(OzArgs args) {
       const int qd = warp & 3;
       const int cbase = ((warp - 2) >> 2) * OZ_ECOLS;
       const uint32_t taddr = c.tbase + ((uint32_t)(qd * 32) << 16) + (uint32_t)cbase;
-      float hi[OZ_ECOLS], lo[OZ_ECOLS];
+      float hi[OZ_ECOLS];
 #pragma unroll
-      for (int j = 0; j < OZ_ECOLS; ++j) {
-        hi[j] = 0.f;
-        lo[j] = 0.f;
+      for (int j = 0; j < OZ_ECOLS; ++j) hi[j] = 0.f;
+      {
+        uint32_t zero[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) zero[j] = 0u;
+        tmem_st16(taddr + 3 * 128, zero);
+        tmem_st16(taddr + 3 * 128 + 16, zero);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
       }
-      int bc = 0;
       uint32_t par = 0;
-      bool ok = oz_fold<0>(args, c, taddr, nks, bc, par, hi, lo) &&
-                oz_fold<1>(args, c, taddr, nks, bc, par, hi, lo) &&
-                (!g3 || oz_fold<2>(args, c, taddr, nks, bc, par, hi, lo));
+      bool ok = oz_fold<0>(args, c, taddr, nks, par, hi) &&
+                oz_fold<1>(args, c, taddr, nks, par, hi) &&
+                (!g3 || oz_fold<2>(args, c, taddr, nks, par, hi));
       if (!ok) {
         *c.abort_flag = 1;
         atomicExch(args.status, 1);
@@ -518,6 +527,10 @@ __global__ void __maxnreg__(112) k_oz_gemm(OzArgs args) {
         ok = false;
       }
       if (ok && !*c.abort_flag) {
+        uint32_t lo[OZ_ECOLS];
+        tmem_ld16(taddr + 3 * 128, lo);
+        tmem_ld16(taddr + 3 * 128 + 16, lo + 16);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
         const int m = mt * OZ_M + qd * 32 + lane;
         if (m < args.M) {
           const int ea = args.eA[m];
@@ -525,7 +538,8 @@ __global__ void __maxnreg__(112) k_oz_gemm(OzArgs args) {
           for (int j = 0; j < OZ_ECOLS; ++j) {
             const int n = nt * OZ_N + cbase + j;
             if (n < args.N) {
-              const double v = oz_scale2((double)hi[j] + (double)lo[j], ea + args.eB[n]);
+              const double v = oz_scale2((double)hi[j] + (double)__uint_as_float(lo[j]),
+                                         ea + args.eB[n]);
               if (MODE == OZ_OUT_PARTIAL)
                 args.out[((size_t)z * args.N + n) * args.M + m] = v;
               else

@@ -346,3 +346,49 @@ def test_df32_transforms_match_fp64_closely(cuda):
         H.hpsi(dev(psi), o, synth.occupations(cell))
         outs[prec] = o.cpu().numpy()
     assert rel_err(outs["mixed_df32"], outs["fp64"]) < 1e-11
+
+
+def species_fixture():
+    """Projector tables of two pseudopotentials of the reference's own test
+    suite (ONCV Xe from UPF, ONCV Ar from QSO XML; s, p, d, two channels),
+    made by the reference's Species code (tests/golden/make_golden.py)."""
+    from conftest import load_golden
+    g = load_golden("species_xe_ar")
+    sp = [dict(tau=g[f"tau{i}"], twnl=g[f"twnl{i}"], lproj=g[f"lproj{i}"], wt=g[f"wt{i}"])
+          for i in range(len(g["names"]))]
+    return g, sp
+
+
+@pytest.mark.parametrize("prec,gemm,tol", [("fp64", "ozaki", 1e-10), ("fp64", "simt", 1e-10),
+                                           ("mixed_df32", None, 2e-6)])
+def test_hpsi_and_etrs_real_pseudopotential_tables(cuda, prec, gemm, tol):
+    """H|psi> and one ETRS step with the projector tables of real
+    pseudopotentials passed through qbg_set_nonlocal_tables, against the
+    oracle fed the identical tables (26 projectors per Xe + Ar pair)."""
+    g, sp = species_fixture()
+    b = Q.Basis(g["a"], float(g["ecut"]))
+    grid = tuple(int(x) for x in g["grid"])
+    A = np.asarray(g["A"])
+    H = Q.Hamiltonian(b, *grid, precision=prec)
+    if gemm:
+        H.set_fp64_gemm(gemm)
+    cell = synth.make_cell("t12")
+    v = synth.vlocal(cell)
+    H.set_vlocal(v)
+    H.set_vector_potential(A)
+    H.set_nonlocal(sp)
+    oft = O.FT(O.Basis(b.a, float(g["ecut"])), *grid)
+    oh = O.Ham(oft, v, sp)
+    oh.set_A(A)
+    psi = synth.wavefunctions(cell, b, nst=6)
+    occ = np.full(6, 2.0)
+    torch = _torch()
+    out = torch.zeros_like(dev(psi))
+    enl = H.hpsi(dev(psi), out, occ, want_enl=True)
+    ref, enl_ref = oh.hpsi(psi.T, occ, nthreads=NT)
+    assert rel_err(out.cpu().numpy(), ref.T) < tol
+    assert abs(enl - enl_ref) <= tol * abs(enl_ref)
+    p = dev(psi)
+    H.etrs_step(p, occ, 0.05)
+    ref2, _, _ = oh.etrs_step(psi.T.copy(), occ, 0.05, A, A, nthreads=NT)
+    assert rel_err(p.cpu().numpy(), ref2.T) < (tol if prec == "fp64" else 5e-5)

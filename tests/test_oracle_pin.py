@@ -88,3 +88,93 @@ def test_oracle_ft_matches_numpy():
     got = ft.backward(c)
     assert np.abs(got - ref).max() <= 1e-13 * np.abs(ref).max()
     assert np.abs(ft.forward(got) - c).max() <= 1e-13
+
+
+def _species_fixture():
+    g = load_golden("species_xe_ar")
+    return g, [dict(tau=g[f"tau{i}"], twnl=g[f"twnl{i}"], lproj=g[f"lproj{i}"], wt=g[f"wt{i}"])
+               for i in range(len(g["names"]))]
+
+
+def test_species_tables_fixture_shapes_and_symmetry():
+    """The testsuite species tables: KB projector count per species (nlm of
+    Species: nchannels * sum_{l != llocal} (2l+1)), l order of
+    NonLocalPotential::init, l = 1 and 2 rows that are the real harmonics times
+    one radial function, and the radial projectors' values at |G| = 0 (zero
+    for l > 0)."""
+    g, sp = _species_fixture()
+    for i, s in enumerate(sp):
+        info = g[f"info{i}"]
+        lmax, lloc, nch, nlm = (int(x) for x in info[:4])
+        assert len(s["lproj"]) == nlm == s["twnl"].shape[0]
+        assert s["twnl"].shape[1] == int(O.Basis(g["a"], float(g["ecut"])).ngw)
+        expect = [l for l in range(lmax + 1) if l != lloc for _ in range(nch)
+                  for _ in range(2 * l + 1)]
+        assert list(s["lproj"]) == expect
+        vn = g[f"vnlg{i}"]
+        for l in range(1, lmax + 1):
+            if l != lloc:
+                assert np.all(vn[l, :, 0] == 0.0)
+        # the three l = 1 rows of a channel square-sum to (3/4pi) v^2
+        r = [k for k, l in enumerate(s["lproj"]) if l == 1][:3]
+        if r:
+            tw = s["twnl"][r]
+            ss = (tw * tw).sum(0)
+            A = g["A"]
+            kq = O.Basis(g["a"], float(g["ecut"])).kpgx.reshape(3, -1) - A[:, None]
+            gmag = np.sqrt((kq * kq).sum(0))
+            lch = [k for k, l in enumerate(s["lproj"]) if l == 1].index(r[0]) // 3
+            v = np.interp(gmag, g[f"vnlg_g{i}"], vn[1, lch])
+            mask = (gmag > 0.5) & (gmag < 3.0)
+            assert np.allclose(ss[mask], 3.0 / (4 * np.pi) * v[mask] ** 2, rtol=2e-2)
+
+
+def test_oracle_table_path_equals_synthetic_path():
+    """The oracle's caller-table path of NonLocalPotential::energy, fed the
+    tables its synthetic path builds, gives the synthetic path's H|psi> and
+    E_nl bit for bit."""
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    cell = synth.make_cell("t12")
+    b = O.Basis(Q.cubic_cell(cell.L), cell.ecut)
+    ft = O.FT(b, *cell.grid)
+    v = synth.vlocal(cell)
+    sp = synth.species(cell)
+    A = synth.kick()
+    h1 = O.Ham(ft, v, sp)
+    h1.set_A(A)
+    na, npr = len(sp[0]["tau"]), (cell.lmax + 1) ** 2
+    rows = [h1.projector(ipr * na) for ipr in range(npr)]
+    sp2 = [dict(tau=sp[0]["tau"], twnl=np.array([r[0] for r in rows]),
+                lproj=np.array([r[1] for r in rows]), wt=np.array([r[2] for r in rows]))]
+    h2 = O.Ham(ft, v, sp2)
+    h2.set_A(A)
+    rng = np.random.default_rng(1)
+    c = rng.standard_normal((b.ngw, 3)) + 1j * rng.standard_normal((b.ngw, 3))
+    occ = np.full(3, 2.0)
+    r1, e1 = h1.hpsi(c, occ)
+    r2, e2 = h2.hpsi(c, occ)
+    assert np.array_equal(r1, r2) and e1 == e2
+
+
+@pytest.mark.skipif(O.ref() is None, reason="reference checker not built here")
+def test_species_tables_fixture_matches_reference_species():
+    """Live pin: the fixture's radial projectors and KB weights are those of
+    the reference's own Species (read and initialised now from the testsuite
+    files)."""
+    import os
+    root = os.environ.get("QBG_REFERENCE", "")
+    g, sp = _species_fixture()
+    path0 = os.path.join(root, "testsuite", "pseudopotentials", str(g["files"][0]))
+    if not root or not os.path.exists(path0):
+        pytest.skip("reference tree not available")
+    for i in range(len(sp)):
+        h = O.ref_species_load(os.path.join(root, "testsuite", "pseudopotentials",
+                                            str(g["files"][i])), 1.0)
+        info = O.ref_species_info(h)
+        assert np.array_equal(info, g[f"info{i}"])
+        gg = g[f"vnlg_g{i}"]
+        for l in range(info[0] + 1):
+            for ic in range(info[2]):
+                assert np.array_equal(O.ref_species_vnlg(h, l, ic, gg), g[f"vnlg{i}"][l, ic])
+        O.ref_species_destroy(h)
