@@ -130,6 +130,20 @@ class Plan {
                            tau.data()),
           "qbg_set_nonlocal");
   }
+  // Real pseudopotential projector tables (NonLocalPotential::update_twnl's
+  // arrays, species after species; see qbg_set_nonlocal_tables)
+  void set_nonlocal_tables(const std::vector<int>& na, const std::vector<int>& npr,
+                           const std::vector<int>& lproj, const std::vector<double>& wt,
+                           const std::vector<double>& twnl, const std::vector<double>& tau) {
+    check(qbg_set_nonlocal_tables(h_, (int)na.size(), na.data(), npr.data(), lproj.data(),
+                                  wt.data(), twnl.data(), tau.data()),
+          "qbg_set_nonlocal_tables");
+  }
+  // projector GEMMs of the plain FP64 form: QBG_GEMM_OZAKI (slices 6 or 7) or
+  // QBG_GEMM_SIMT
+  void set_fp64_gemm(int mode, int slices = 7) {
+    check(qbg_plan_set_fp64_gemm(h_, mode, slices), "qbg_plan_set_fp64_gemm");
+  }
   void set_vector_potential(const std::array<double, 3>& A) {
     check(qbg_set_vector_potential(h_, A.data()), "qbg_set_vector_potential");
   }

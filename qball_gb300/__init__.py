@@ -82,6 +82,8 @@ ABI = {
     "qbg_etrs_graph_check": [_P],
     "qbg_etrs_graph_destroy": [_P],
     "qbg_plan_autotune": [_P, _P, _I, _I, _P, _P, _P],
+    "qbg_plan_set_transform_config": [_P, _I, _I, _I, _I],
+    "qbg_plan_get_transform_config": [_P, _P],
     "qbg_selftest_wait_timeout": [_I],
     "qbg_plan_set_wait_polls": [_P, _I],
     "qbg_launch_count": [_P, _P],
@@ -242,6 +244,19 @@ class FourierTransform:
         m = {"simt": QBG_GEMM_SIMT, "ozaki": QBG_GEMM_OZAKI}[mode]
         _check(lib().qbg_plan_set_fp64_gemm(self.h, m, int(slices)), "qbg_plan_set_fp64_gemm")
         self.fp64_gemm, self.oz_slices = mode, int(slices)
+
+    def set_transform_config(self, radix_order=0, prime_factor=1, fused=1, lane_group=1):
+        _check(lib().qbg_plan_set_transform_config(self.h, int(radix_order), int(prime_factor),
+                                                   int(fused), int(lane_group)),
+               "qbg_plan_set_transform_config")
+
+    def transform_config(self):
+        """{chunk, radix_order, prime_factor, fused, lane_group}"""
+        c = np.zeros(5, np.int32)
+        _check(lib().qbg_plan_get_transform_config(self.h, _np_ptr(c)),
+               "qbg_plan_get_transform_config")
+        return dict(zip(("chunk", "radix_order", "prime_factor", "fused", "lane_group"),
+                        c.tolist()))
 
     def set_chunk(self, n):
         _check(lib().qbg_plan_set_chunk(self.h, int(n)), "qbg_plan_set_chunk")

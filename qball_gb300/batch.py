@@ -43,6 +43,16 @@ def batch_cells(n, seed):
     return out
 
 
+def _shape_counts(cfgs):
+    """How many plans the autotuner put on each transform shape."""
+    out = {}
+    for c in cfgs:
+        k = (f"order{c['radix_order']}-pfa{c['prime_factor']}-fused{c['fused']}-"
+             f"lane{c['lane_group']}-chunk{c['chunk']}")
+        out[k] = out.get(k, 0) + 1
+    return dict(sorted(out.items()))
+
+
 def main():
     import torch
     import qball_gb300 as Q
@@ -54,6 +64,10 @@ def main():
     ap.add_argument("--form", default="mixed_df32")
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--dt", type=float, default=0.05)
+    ap.add_argument("--compare", default="",
+                    help="comma-separated forms whose per-cell error after --compare-steps "
+                         "ETRS steps is measured against the FP64 form (e.g. mixed,mixed_df32)")
+    ap.add_argument("--compare-steps", type=int, default=2)
     args = ap.parse_args()
     torch.cuda.set_device(0)
     specs = batch_cells(args.cells, args.seed)
@@ -117,10 +131,60 @@ def main():
         "graph_speedup": ms_seq / ms_graph,
         "max_rel_diff_graph_vs_sequential": diff,
         "chunks": sorted({H.chunk for H, _, _ in bat}),
+        "transform_shapes": _shape_counts([H.transform_config() for H, _, _ in bat]),
         "setup_s": setup_s,
         "device_gb_in_use": (lambda f: (f[1] - f[0]) / 1e9)(torch.cuda.mem_get_info()),
     }
+    if args.compare:
+        del seq, bat, graph
+        torch.cuda.empty_cache()
+        line["per_cell_error"] = compare_forms(specs, args)
     print(json.dumps(line), flush=True)
+
+
+def compare_forms(specs, args):
+    """Per cell: relative error of psi and of the current J after a few ETRS
+    steps of each reduced form against the FP64 form (complex128 storage and
+    arithmetic, tensor-core FP64-accurate projector GEMMs) on the same cell,
+    one cell at a time."""
+    import torch
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    forms = [f for f in args.compare.split(",") if f]
+    A = synth.kick()
+    rows = []
+    for i, (L, ecut, g, natoms, nst) in enumerate(specs):
+        cell = synth.make_cell(None, seed=args.seed * 1000 + i, L=L, ecut=ecut, grid=(g, g, g),
+                               nst=nst, natoms=natoms, lmax=1)
+        b = Q.Basis(cell.L, cell.ecut)
+        psi0 = torch.from_numpy(synth.wavefunctions(cell, b)).cuda()
+        occ = synth.occupations(cell)
+        out = {}
+        for form in ["fp64"] + forms:
+            H = Q.Hamiltonian(b, *cell.grid, precision=form)
+            H.set_vlocal(synth.vlocal(cell))
+            H.set_nonlocal(synth.species(cell))
+            H.set_vector_potential(A)
+            p = psi0.clone()
+            for _ in range(args.compare_steps):
+                H.etrs_step(p, occ, args.dt)
+            out[form] = (p, H.current(p, occ, float(occ.sum())))
+            H.close()
+        p64, J64 = out["fp64"]
+        row = {"grid": g, "nst": nst, "natoms": natoms}
+        for form in forms:
+            p, J = out[form]
+            row[form] = {"psi": float(((p - p64).abs().pow(2).sum().sqrt()
+                                       / p64.abs().pow(2).sum().sqrt()).item()),
+                         "J": float(np.abs(J - J64).max() / max(np.abs(J64).max(), 1e-300))}
+        rows.append(row)
+        del out, psi0
+        torch.cuda.empty_cache()
+    summary = {f: {"psi_max": max(r[f]["psi"] for r in rows),
+                   "psi_median": float(np.median([r[f]["psi"] for r in rows])),
+                   "J_max": max(r[f]["J"] for r in rows)} for f in forms}
+    return {"steps": args.compare_steps, "reference": "fp64 form", "summary": summary,
+            "cells": rows}
 
 
 if __name__ == "__main__":

@@ -1097,6 +1097,7 @@ static qbg_status run_xyx(qbg_plan* p, int ns, int G, size_t sm, cudaStream_t st
 template <typename T> static int xyx_group(const qbg_plan* p, size_t* smem) {
   const FFTLen<T> dx = p->len[0].view<T>(), dy = p->len[1].view<T>();
   if (!p->fuse_xyx || !xyx_lengths(p->np0, p->np1) || std::is_same<T, float>::value) return 0;
+  if (!dx.pfa || !dy.pfa) return 0;  // the fused kernel runs prime-factor splits in place
   const size_t cs = sizeof(cplx<T>);
   const size_t base = (size_t)p->nband * (p->np0 + 1) * cs;
   const size_t per_col = (size_t)(p->np1 + 1) * cs + (size_t)p->np1 * sizeof(T);
@@ -1115,6 +1116,7 @@ template <typename T> static int xyx_group(const qbg_plan* p, size_t* smem) {
 template <typename T> static int xy_density_group(const qbg_plan* p, size_t* smem) {
   if (!p->fuse_xyx || !xyx_lengths(p->np0, p->np1) || std::is_same<T, float>::value) return 0;
   const FFTLen<T> dy = p->len[1].view<T>();
+  if (!dy.pfa || !p->len[0].view<T>().pfa) return 0;
   const size_t cs = sizeof(cplx<T>);
   const size_t base = (size_t)p->nband * (p->np0 + 1) * cs;
   const size_t per_col = (size_t)(p->np1 + 1) * cs + (size_t)p->np1 * sizeof(double);

@@ -185,27 +185,63 @@ qbg_status qbg_plan_autotune(qbg_plan* p, const double* psi, int ld, int nst, co
   cudaEvent_t a, b;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
-  const int old = p->chunk;
-  int best = old;
-  float best_ms = 1e30f;
   qbg_status s = QBG_OK;
-  for (int ch : {8, 16, 32, 64}) {
-    if (ch > 2 * nst && ch != 8) break;
-    p->chunk = ch;
-    s = qbg_hpsi(p, psi, ld, out, nst, occ, nullptr, stream);  // warm-up (allocations)
-    if (s != QBG_OK) break;
+  // device time of two H|psi> after a warm-up (which also grows the scratch)
+  auto time_h = [&](float* ms) -> qbg_status {
+    qbg_status r = qbg_hpsi(p, psi, ld, out, nst, occ, nullptr, stream);
+    if (r != QBG_OK) return r;
     cudaEventRecord(a, st);
-    for (int r = 0; r < 2 && s == QBG_OK; ++r) s = qbg_hpsi(p, psi, ld, out, nst, occ, nullptr, stream);
+    for (int k = 0; k < 2 && r == QBG_OK; ++k) r = qbg_hpsi(p, psi, ld, out, nst, occ, nullptr, stream);
     cudaEventRecord(b, st);
     cudaEventSynchronize(b);
+    *ms = 0.f;
+    cudaEventElapsedTime(ms, a, b);
+    return r;
+  };
+  int cfg0[5];
+  qbg_plan_get_transform_config(p, cfg0);
+  // 1) transform shape at the current chunk: radix order of the Stockham
+  //    passes, prime-factor splits, the fused x-y-x kernel, the
+  //    register lane-group y pass (FP32 transforms only)
+  int best[4] = {cfg0[1], cfg0[2], cfg0[3], cfg0[4]};
+  float best_ms = 1e30f;
+  const bool fp32 = p->prec == QBG_PREC_MIXED || p->prec == QBG_PREC_MIXED_NL64;
+  for (int order = 0; order < 3 && s == QBG_OK; ++order)
+    for (int pfa = 1; pfa >= 0 && s == QBG_OK; --pfa)
+      for (int fused = 1; fused >= 0 && s == QBG_OK; --fused)
+        for (int lane = 1; lane >= (fp32 ? 0 : 1) && s == QBG_OK; --lane) {
+          if (!pfa && fused) continue;  // the fused kernels need the prime-factor splits
+          s = qbg_plan_set_transform_config(p, order, pfa, fused, lane);
+          float ms = 0.f;
+          if (s == QBG_OK) s = time_h(&ms);
+          if (s == QBG_OK && ms < best_ms) {
+            best_ms = ms;
+            best[0] = order;
+            best[1] = pfa;
+            best[2] = fused;
+            best[3] = lane;
+          }
+        }
+  if (s == QBG_OK) s = qbg_plan_set_transform_config(p, best[0], best[1], best[2], best[3]);
+  // 2) states per transform launch group with that shape
+  int best_ch = cfg0[0];
+  best_ms = 1e30f;
+  for (int ch : {8, 16, 32, 64}) {
+    if (s != QBG_OK || (ch > 2 * nst && ch != 8)) break;
+    p->chunk = ch;
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
+    s = time_h(&ms);
     if (s == QBG_OK && ms < best_ms) {
       best_ms = ms;
-      best = ch;
+      best_ch = ch;
     }
   }
-  p->chunk = s == QBG_OK ? best : old;
+  if (s == QBG_OK) {
+    p->chunk = best_ch;
+  } else {
+    p->chunk = cfg0[0];
+    qbg_plan_set_transform_config(p, cfg0[1], cfg0[2], cfg0[3], cfg0[4]);
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   cudaFree(out);

@@ -44,6 +44,7 @@ struct LenTables {
   double2* d_root64 = nullptr;  // exp(-2 pi i m / n), m < n
   float2* d_root32 = nullptr;
   df32c* d_rootdf = nullptr;
+  bool allow_pfa = true;  // prime-factor in-place split where the length has one
   template <typename T> FFTLen<T> view() const;
 };
 
@@ -112,6 +113,8 @@ struct qbg_plan {
   size_t anl_elems = 0;        // nproj * ngw of d_anl
   long long nl_version = 0;    // incremented by every table build
   void* d_pdesc = nullptr;     // [nproj] projector descriptors (qbg_nl.cu)
+  void* d_adesc = nullptr;     // [nl_natoms] atom descriptors (qbg_nl.cu)
+  int nl_natoms = 0;
   float2* d_anl32 = nullptr;   // [nproj][ngw] FP32 copy (mixed)
   bool nl_ready = false;
   void* tc = nullptr;          // tensor-core projector tables (mixed)
@@ -122,6 +125,7 @@ struct qbg_plan {
   int tc_polls = -1;            // poll limit of the GEMM pipeline waits (-1: default)
   bool lane_fft = true;         // register-resident lane-group transforms where supported
   bool fuse_xyx = true;         // x, y and x passes of H psi in one kernel where they fit
+  int radix_order = 0;          // Stockham radix order of the length tables (factorize)
 
   // scratch (allocated lazily, grown as needed)
   void* d_Z = nullptr;  size_t Z_bytes = 0;   // [chunk][n2][nrods]

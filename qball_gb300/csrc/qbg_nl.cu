@@ -28,71 +28,81 @@ struct ProjDesc {
   int row;
 };
 
+// One atom's projectors: p = p0 + ipr * stride for ipr < npr (the index
+// ia + ipr*nblk of NonLocalPotential.cc:2000 inside the atom's block).
+struct AtomDesc {
+  int p0, stride, npr, pad;
+  double rc;
+  double tau[3];
+};
+
 // update_twnl (NonLocalPotential.cc:306-760) for the synthetic radial form,
-// evaluated at k+G-A, times (-i)^l exp(-i (k+G-A).tau)  (:1962-2037).
-// With caller tables (pd[p].row >= 0) the factor twnl[row][g] is taken as
-// given, for l = 0..3.
-template <bool MIXED>
+// evaluated at k+G-A, times (-i)^l exp(-i (k+G-A).tau)  (:1962-2037).  One
+// thread per (G, atom): the structure phase, |k+G-A| and the radial
+// Gaussian are computed once and shared by the atom's projectors (FP64
+// transcendentals are the cost of this kernel on GB300).  With caller
+// tables (pd[p].row >= 0) the factor twnl[row][g] is taken as given, for
+// l = 0..3.
 __global__ void k_anl(const double* __restrict__ kpgx, const double* __restrict__ kpg2A,
                       int ngw, double A0, double A1, double A2,
-                      const ProjDesc* __restrict__ pd, int nproj,
-                      const double* __restrict__ twnl,
-                      double2* __restrict__ anl, float2* __restrict__ anl32) {
+                      const AtomDesc* __restrict__ ad, const ProjDesc* __restrict__ pd,
+                      const double* __restrict__ twnl, double2* __restrict__ anl) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  const int p = blockIdx.y;
-  if (g >= ngw || p >= nproj) return;
-  const ProjDesc d = pd[p];
+  if (g >= ngw) return;
+  const AtomDesc at = ad[blockIdx.y];
   const double kx = kpgx[g] - A0, ky = kpgx[ngw + g] - A1, kz = kpgx[2 * ngw + g] - A2;
   const double k2 = kpg2A[g];
   const double tg = sqrt(k2);
   const double tgi = k2 > 0.0 ? 1.0 / sqrt(k2) : 0.0;
-  const double e = exp(-0.5 * tg * tg * d.rc * d.rc);
+  const double e = exp(-0.5 * tg * tg * at.rc * at.rc);
   const double pi = 3.14159265358979323846, fpi = 4.0 * pi;
-  double t;
-  if (d.row >= 0) {
-    t = twnl[(size_t)d.row * ngw + g];
-  } else if (d.l == 0) {
-    t = sqrt(1.0 / fpi) * e;
-  } else if (d.l == 1) {
-    const double s34pi = sqrt(3.0 / fpi);
-    const double c = d.m == 0 ? kx : (d.m == 1 ? ky : kz);
-    t = (s34pi * c * tgi) * (tg * e);
-  } else {
-    const double s54pi = sqrt(5.0 / fpi), s3 = sqrt(3.0);
-    const double tgi2 = tgi * tgi;
-    double y;
-    switch (d.m) {
-      case 0: y = s54pi * 0.5 * (3.0 * (kz * kz * tgi2) - 1.0); break;
-      case 1: y = s54pi * 0.5 * s3 * (kx * kx * tgi2 - ky * ky * tgi2); break;
-      case 2: y = s54pi * s3 * (kx * ky * tgi2); break;
-      case 3: y = s54pi * s3 * (ky * kz * tgi2); break;
-      default: y = s54pi * s3 * (kx * kz * tgi2); break;
-    }
-    t = y * (tg * tg * e);
-  }
   // kpgr = -(k+G-A).tau, rounded term by term as the reference's dgemm
-  double kpgr = __dmul_rn(-d.tau[0], kx);
-  kpgr = __dadd_rn(kpgr, __dmul_rn(-d.tau[1], ky));
-  kpgr = __dadd_rn(kpgr, __dmul_rn(-d.tau[2], kz));
+  double kpgr = __dmul_rn(-at.tau[0], kx);
+  kpgr = __dadd_rn(kpgr, __dmul_rn(-at.tau[1], ky));
+  kpgr = __dadd_rn(kpgr, __dmul_rn(-at.tau[2], kz));
   double s, c;
   sincos(kpgr, &s, &c);
-  double re, im;
-  if (d.l == 0) {
-    re = t * c;
-    im = t * s;
-  } else if (d.l == 1) {
-    re = t * s;
-    im = -t * c;
-  } else if (d.l == 2) {
-    re = -t * c;
-    im = -t * s;
-  } else {
-    re = -t * s;
-    im = t * c;
+  for (int ipr = 0; ipr < at.npr; ++ipr) {
+    const int p = at.p0 + ipr * at.stride;
+    const ProjDesc d = pd[p];
+    double t;
+    if (d.row >= 0) {
+      t = twnl[(size_t)d.row * ngw + g];
+    } else if (d.l == 0) {
+      t = sqrt(1.0 / fpi) * e;
+    } else if (d.l == 1) {
+      const double s34pi = sqrt(3.0 / fpi);
+      const double cm = d.m == 0 ? kx : (d.m == 1 ? ky : kz);
+      t = (s34pi * cm * tgi) * (tg * e);
+    } else {
+      const double s54pi = sqrt(5.0 / fpi), s3 = sqrt(3.0);
+      const double tgi2 = tgi * tgi;
+      double y;
+      switch (d.m) {
+        case 0: y = s54pi * 0.5 * (3.0 * (kz * kz * tgi2) - 1.0); break;
+        case 1: y = s54pi * 0.5 * s3 * (kx * kx * tgi2 - ky * ky * tgi2); break;
+        case 2: y = s54pi * s3 * (kx * ky * tgi2); break;
+        case 3: y = s54pi * s3 * (ky * kz * tgi2); break;
+        default: y = s54pi * s3 * (kx * kz * tgi2); break;
+      }
+      t = y * (tg * tg * e);
+    }
+    double re, im;
+    if (d.l == 0) {
+      re = t * c;
+      im = t * s;
+    } else if (d.l == 1) {
+      re = t * s;
+      im = -t * c;
+    } else if (d.l == 2) {
+      re = -t * c;
+      im = -t * s;
+    } else {
+      re = -t * s;
+      im = t * c;
+    }
+    anl[(size_t)p * ngw + g] = make_double2(re, im);
   }
-  const size_t o = (size_t)p * ngw + g;
-  anl[o] = make_double2(re, im);
-  if (MIXED) anl32[o] = make_float2((float)re, (float)im);
 }
 
 __global__ void k_kpg2A(const double* __restrict__ kpgx, int ngw, double A0, double A1,
@@ -122,7 +132,8 @@ qbg_status update_kinetic(qbg_plan* p, cudaStream_t st) {
 // projector order: species, atom blocks of <= 128 atoms, projector ipr
 // (l, then m), atom within the block -- the index ia + ipr*nblk of
 // NonLocalPotential.cc:2000 taken block by block.
-static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector<double>& wt) {
+static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector<double>& wt,
+                       std::vector<AtomDesc>& ad) {
   int namax = 0;
   for (int s = 0; s < p->nsp; ++s) namax = std::max(namax, p->sp_na[s]);
   const int nbs = std::max(1, std::min(namax, 128));
@@ -134,6 +145,16 @@ static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector
       const int na = p->sp_na[s], npr = p->sp_npr[s];
       for (int b0 = 0; b0 < na; b0 += nbs) {
         const int b1 = std::min(na, b0 + nbs);
+        for (int ia = b0; ia < b1; ++ia) {
+          AtomDesc a;
+          a.p0 = (int)pd.size() + (ia - b0);
+          a.stride = b1 - b0;
+          a.npr = npr;
+          a.pad = 0;
+          a.rc = 0.0;
+          for (int j = 0; j < 3; ++j) a.tau[j] = p->sp_tau[3 * (size_t)(atom0 + ia) + j];
+          if (npr > 0) ad.push_back(a);
+        }
         for (int ipr = 0; ipr < npr; ++ipr)
           for (int ia = b0; ia < b1; ++ia) {
             ProjDesc d;
@@ -156,6 +177,16 @@ static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector
     const int na = p->sp_na[s], lmax = p->sp_lmax[s];
     for (int b0 = 0; b0 < na; b0 += nbs) {
       const int b1 = std::min(na, b0 + nbs);
+      for (int ia = b0; ia < b1; ++ia) {
+        AtomDesc a;
+        a.p0 = (int)pd.size() + (ia - b0);
+        a.stride = b1 - b0;
+        a.npr = (lmax + 1) * (lmax + 1);
+        a.pad = 0;
+        a.rc = p->sp_rc[s];
+        for (int j = 0; j < 3; ++j) a.tau[j] = p->sp_tau[3 * (size_t)(atom0 + ia) + j];
+        if (a.npr > 0) ad.push_back(a);
+      }
       for (int l = 0; l <= lmax; ++l)
         for (int m = 0; m < 2 * l + 1; ++m)
           for (int ia = b0; ia < b1; ++ia) {
@@ -181,7 +212,8 @@ static void proj_descs(const qbg_plan* p, std::vector<ProjDesc>& pd, std::vector
 qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
   std::vector<ProjDesc> pd;
   std::vector<double> wt;
-  proj_descs(p, pd, wt);
+  std::vector<AtomDesc> ad;
+  proj_descs(p, pd, wt, ad);
   const int P = (int)pd.size();
   const size_t n = (size_t)P * p->ngw;
   const bool same = P == p->nproj && p->d_anl && p->anl_elems == n && n > 0;
@@ -193,7 +225,7 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
   } else {
     tc_release(p);
     oz_release(p);
-    void* bufs[] = {p->d_ptau, p->d_pwt, p->d_anl, p->d_anl32, p->d_pdesc};
+    void* bufs[] = {p->d_ptau, p->d_pwt, p->d_anl, p->d_anl32, p->d_pdesc, p->d_adesc};
     for (void* b : bufs)
       if (b) cudaFree(b);
     p->d_ptau = nullptr;
@@ -201,14 +233,17 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
     p->d_anl = nullptr;
     p->d_anl32 = nullptr;
     p->d_pdesc = nullptr;
+    p->d_adesc = nullptr;
     p->anl_elems = 0;
   }
+  p->nl_natoms = (int)ad.size();
   p->nproj = P;
   p->nl_ready = true;
   p->nl_version++;
   if (P == 0 || p->ngw == 0) return QBG_OK;
   if (!same) {
     QBG_CUDA(cudaMalloc(&p->d_pdesc, sizeof(ProjDesc) * P));
+    QBG_CUDA(cudaMalloc(&p->d_adesc, sizeof(AtomDesc) * ad.size()));
     QBG_CUDA(cudaMalloc(&p->d_pwt, sizeof(double) * P));
     QBG_CUDA(cudaMalloc(&p->d_anl, sizeof(double2) * n));
     p->anl_elems = n;
@@ -216,10 +251,12 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
   // pageable host sources: these copies complete before returning
   QBG_CUDA(cudaMemcpy(p->d_pdesc, pd.data(), sizeof(ProjDesc) * P, cudaMemcpyHostToDevice));
   QBG_CUDA(cudaMemcpy(p->d_pwt, wt.data(), sizeof(double) * P, cudaMemcpyHostToDevice));
-  dim3 grid((p->ngw + 255) / 256, P);
-  k_anl<false><<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
-                                     (const ProjDesc*)p->d_pdesc, P, p->d_twnl, p->d_anl,
-                                     nullptr);
+  QBG_CUDA(cudaMemcpy(p->d_adesc, ad.data(), sizeof(AtomDesc) * ad.size(),
+                      cudaMemcpyHostToDevice));
+  dim3 grid((p->ngw + 255) / 256, (unsigned)ad.size());
+  k_anl<<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2],
+                              (const AtomDesc*)p->d_adesc, (const ProjDesc*)p->d_pdesc,
+                              p->d_twnl, p->d_anl);
   p->launches++;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -454,49 +491,53 @@ template qbg_status nl_apply<double>(qbg_plan*, const double2*, int, double2*, i
 //   e.grad t = s_l (e.grad P - rc^2 P (e.q)) exp(-|q|^2 rc^2 / 2).
 __global__ void k_anl_da(const double* __restrict__ kpgx, const double* __restrict__ kpg2A,
                          int ngw, double A0, double A1, double A2, double e0, double e1,
-                         double e2, const ProjDesc* __restrict__ pd, int nproj,
-                         double2* __restrict__ dbeta) {
+                         double e2, const AtomDesc* __restrict__ ad,
+                         const ProjDesc* __restrict__ pd, double2* __restrict__ dbeta) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
-  const int p = blockIdx.y;
-  if (g >= ngw || p >= nproj) return;
-  const ProjDesc d = pd[p];
+  if (g >= ngw) return;
+  const AtomDesc at = ad[blockIdx.y];
   const double qx = kpgx[g] - A0, qy = kpgx[ngw + g] - A1, qz = kpgx[2 * ngw + g] - A2;
-  const double rc2 = d.rc * d.rc;
+  const double rc2 = at.rc * at.rc;
   const double E = exp(-0.5 * kpg2A[g] * rc2);
   const double eq = e0 * qx + e1 * qy + e2 * qz;
   const double fpi = 4.0 * 3.14159265358979323846;
-  double P, eP, s;
-  if (d.l == 0) {
-    s = sqrt(1.0 / fpi);
-    P = 1.0;
-    eP = 0.0;
-  } else if (d.l == 1) {
-    s = sqrt(3.0 / fpi);
-    P = d.m == 0 ? qx : (d.m == 1 ? qy : qz);
-    eP = d.m == 0 ? e0 : (d.m == 1 ? e1 : e2);
-  } else {
-    const double s3 = sqrt(3.0);
-    s = sqrt(5.0 / fpi);
-    switch (d.m) {
-      case 0: P = 0.5 * (2.0 * qz * qz - qx * qx - qy * qy);
-              eP = -e0 * qx - e1 * qy + 2.0 * e2 * qz; break;
-      case 1: P = 0.5 * s3 * (qx * qx - qy * qy); eP = s3 * (e0 * qx - e1 * qy); break;
-      case 2: P = s3 * qx * qy; eP = s3 * (e0 * qy + e1 * qx); break;
-      case 3: P = s3 * qy * qz; eP = s3 * (e1 * qz + e2 * qy); break;
-      default: P = s3 * qx * qz; eP = s3 * (e0 * qz + e2 * qx); break;
-    }
-  }
-  const double t = s * P * E;
-  const double wr = s * E * (eP - rc2 * P * eq);
-  const double wi = -(e0 * d.tau[0] + e1 * d.tau[1] + e2 * d.tau[2]) * t;
+  const double etau = e0 * at.tau[0] + e1 * at.tau[1] + e2 * at.tau[2];
   double sn, cs;
-  sincos(-(d.tau[0] * qx + d.tau[1] * qy + d.tau[2] * qz), &sn, &cs);
-  const double zr = cs * wr - sn * wi, zi = sn * wr + cs * wi;
-  double2 o;
-  if (d.l == 0) o = make_double2(-zr, -zi);
-  else if (d.l == 1) o = make_double2(-zi, zr);
-  else o = make_double2(zr, zi);
-  dbeta[(size_t)p * ngw + g] = o;
+  sincos(-(at.tau[0] * qx + at.tau[1] * qy + at.tau[2] * qz), &sn, &cs);
+  for (int ipr = 0; ipr < at.npr; ++ipr) {
+    const int p = at.p0 + ipr * at.stride;
+    const ProjDesc d = pd[p];
+    double P, eP, s;
+    if (d.l == 0) {
+      s = sqrt(1.0 / fpi);
+      P = 1.0;
+      eP = 0.0;
+    } else if (d.l == 1) {
+      s = sqrt(3.0 / fpi);
+      P = d.m == 0 ? qx : (d.m == 1 ? qy : qz);
+      eP = d.m == 0 ? e0 : (d.m == 1 ? e1 : e2);
+    } else {
+      const double s3 = sqrt(3.0);
+      s = sqrt(5.0 / fpi);
+      switch (d.m) {
+        case 0: P = 0.5 * (2.0 * qz * qz - qx * qx - qy * qy);
+                eP = -e0 * qx - e1 * qy + 2.0 * e2 * qz; break;
+        case 1: P = 0.5 * s3 * (qx * qx - qy * qy); eP = s3 * (e0 * qx - e1 * qy); break;
+        case 2: P = s3 * qx * qy; eP = s3 * (e0 * qy + e1 * qx); break;
+        case 3: P = s3 * qy * qz; eP = s3 * (e1 * qz + e2 * qy); break;
+        default: P = s3 * qx * qz; eP = s3 * (e0 * qz + e2 * qx); break;
+      }
+    }
+    const double t = s * P * E;
+    const double wr = s * E * (eP - rc2 * P * eq);
+    const double wi = -etau * t;
+    const double zr = cs * wr - sn * wi, zi = sn * wr + cs * wi;
+    double2 o;
+    if (d.l == 0) o = make_double2(-zr, -zi);
+    else if (d.l == 1) o = make_double2(-zi, zr);
+    else o = make_double2(zr, zi);
+    dbeta[(size_t)p * ngw + g] = o;
+  }
 }
 
 qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_t st) {
@@ -510,9 +551,10 @@ qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_
     set_error("projector derivative: the projector table is not built");
     return QBG_ERR_STATE;
   }
-  dim3 grid((p->ngw + 255) / 256, p->nproj);
+  dim3 grid((p->ngw + 255) / 256, (unsigned)p->nl_natoms);
   k_anl_da<<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2], e[0],
-                                 e[1], e[2], (const ProjDesc*)p->d_pdesc, p->nproj, dbeta);
+                                 e[1], e[2], (const AtomDesc*)p->d_adesc,
+                                 (const ProjDesc*)p->d_pdesc, dbeta);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }

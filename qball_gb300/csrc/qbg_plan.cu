@@ -192,18 +192,37 @@ bool is_codelet(int r) {
   }
 }
 
-// Greedy 8/4/2/odd-prime split.  (Two-pass splits with the 9..16-point
-// codelets were measured slower on GB300: the larger codelets raise the
-// register count of every transform kernel and cut its occupancy.)
-bool factorize(int n, LenTables& L) {
+// Radix orders of the Stockham passes (the autotuner's choice):
+//   0: greedy 8/4/2, then the odd primes (default);
+//   1: the odd primes first, then 8/4/2;
+//   2: radix 4 preferred (4s, then 2), then the odd primes.
+// (Two-pass splits with the 9..16-point codelets were measured slower on
+// GB300: the larger codelets raise the register count of every transform
+// kernel and cut its occupancy.)
+bool factorize(int n, LenTables& L, int order) {
   int r[16], np = 0;
   {
     int m = n;
-    while (m % 8 == 0 && m > 1 && np < 16) { r[np++] = 8; m /= 8; }
-    if (m % 4 == 0) { r[np++] = 4; m /= 4; }
-    if (m % 2 == 0) { r[np++] = 2; m /= 2; }
-    for (int q : {3, 5, 7, 11, 13})
-      while (m % q == 0 && np < 16) { r[np++] = q; m /= q; }
+    auto odd = [&]() {
+      for (int q : {3, 5, 7, 11, 13})
+        while (m % q == 0 && np < 16) { r[np++] = q; m /= q; }
+    };
+    auto pow2 = [&]() {
+      if (order == 2) {
+        while (m % 4 == 0 && m > 1 && np < 16) { r[np++] = 4; m /= 4; }
+      } else {
+        while (m % 8 == 0 && m > 1 && np < 16) { r[np++] = 8; m /= 8; }
+        if (m % 4 == 0) { r[np++] = 4; m /= 4; }
+      }
+      if (m % 2 == 0) { r[np++] = 2; m /= 2; }
+    };
+    if (order == 1) {
+      odd();
+      pow2();
+    } else {
+      pow2();
+      odd();
+    }
     if (m != 1) return false;
   }
   if (np > kMaxPass) return false;
@@ -229,8 +248,8 @@ void unit_root(long long t, long long M, double* re, double* im) {
   *im = (double)-std::sin(ang);
 }
 
-qbg_status build_len(int n, LenTables& L) {
-  if (!factorize(n, L)) {
+qbg_status build_len(int n, LenTables& L, int order) {
+  if (!factorize(n, L, order)) {
     set_error("grid length %d has a prime factor outside {2,3,5,7,11,13} or too many passes", n);
     return QBG_ERR_UNSUPPORTED;
   }
@@ -362,7 +381,7 @@ template <> FFTLen<double> LenTables::view<double>() const {
   d.goff7 = goff7;
   d.goff11 = goff11;
   d.goff13 = goff13;
-  d.pfa = pfa_split(n);
+  d.pfa = allow_pfa ? pfa_split(n) : 0;
   return d;
 }
 template <> FFTLen<df32> LenTables::view<df32>() const {
@@ -383,7 +402,7 @@ template <> FFTLen<df32> LenTables::view<df32>() const {
   d.goff7 = goff7;
   d.goff11 = goff11;
   d.goff13 = goff13;
-  d.pfa = pfa_split(n);
+  d.pfa = allow_pfa ? pfa_split(n) : 0;
   return d;
 }
 template <> FFTLen<float> LenTables::view<float>() const {
@@ -404,7 +423,7 @@ template <> FFTLen<float> LenTables::view<float>() const {
   d.goff7 = goff7;
   d.goff11 = goff11;
   d.goff13 = goff13;
-  d.pfa = pfa_split(n);
+  d.pfa = allow_pfa ? pfa_split(n) : 0;
   return d;
 }
 
@@ -490,7 +509,7 @@ qbg_status qbg_plan_destroy(qbg_plan* p) {
   for (auto& L : p->len) free_len(L);
   void* bufs[] = {p->d_rods, p->d_row_ptr, p->d_row_rod, p->d_row_x, p->d_band_y,
                   p->d_kpgx, p->d_kpg2A, p->d_kpg2A32, p->d_vr, p->d_vr32, p->d_vrdf,
-                  p->d_plist, p->d_ptau, p->d_pwt, p->d_pl, p->d_prc, p->d_pdesc,
+                  p->d_plist, p->d_ptau, p->d_pwt, p->d_pl, p->d_prc, p->d_pdesc, p->d_adesc,
                   p->d_anl, p->d_anl32, p->d_twnl, p->d_Z, p->d_Y, p->d_fnl, p->d_fpart,
                   p->d_red, p->d_rho, p->d_rho_slots, p->d_vsph, p->d_w[0], p->d_w[1], p->d_w[2], p->d_w[3]};
   for (void* b : bufs)
@@ -558,7 +577,7 @@ qbg_status qbg_plan_create(const qbg_basis_desc* bd, int np0, int np1, int np2,
   }
   const int ns[3] = {np0, np1, np2};
   for (int d = 0; d < 3; ++d) {
-    qbg_status s = build_len(ns[d], p->len[d]);
+    qbg_status s = build_len(ns[d], p->len[d], 0);
     if (s != QBG_OK) {
       qbg_plan_destroy(p);
       return s;
@@ -628,6 +647,46 @@ qbg_status qbg_plan_set_chunk(qbg_plan* p, int states) {
     return QBG_ERR_INVALID;
   }
   p->chunk = states;
+  return QBG_OK;
+}
+
+qbg_status qbg_plan_set_transform_config(qbg_plan* p, int radix_order, int prime_factor,
+                                         int fused, int lane_group) {
+  if (!p || radix_order < 0 || radix_order > 2) {
+    set_error("qbg_plan_set_transform_config: radix_order must be 0, 1 or 2");
+    return QBG_ERR_INVALID;
+  }
+  if (radix_order != p->radix_order) {
+    QBG_CUDA(cudaDeviceSynchronize());  // kernels may still read the old tables
+    const int ns[3] = {p->np0, p->np1, p->np2};
+    for (int d = 0; d < 3; ++d) {
+      LenTables L;
+      qbg_status s = build_len(ns[d], L, radix_order);
+      if (s != QBG_OK) {
+        free_len(L);
+        return s;
+      }
+      free_len(p->len[d]);
+      p->len[d] = L;
+    }
+    p->radix_order = radix_order;
+  }
+  for (auto& L : p->len) L.allow_pfa = prime_factor != 0;
+  p->fuse_xyx = fused != 0;
+  p->lane_fft = lane_group != 0;
+  return QBG_OK;
+}
+
+qbg_status qbg_plan_get_transform_config(const qbg_plan* p, int* cfg) {
+  if (!p || !cfg) {
+    set_error("qbg_plan_get_transform_config: null argument");
+    return QBG_ERR_INVALID;
+  }
+  cfg[0] = p->chunk;
+  cfg[1] = p->radix_order;
+  cfg[2] = p->len[0].allow_pfa ? 1 : 0;
+  cfg[3] = p->fuse_xyx ? 1 : 0;
+  cfg[4] = p->lane_fft ? 1 : 0;
   return QBG_OK;
 }
 

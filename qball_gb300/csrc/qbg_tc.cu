@@ -78,10 +78,6 @@ __device__ __forceinline__ void split2(float x, __half& hi, __half& lo) {
   hi = __float2half_rn(x);
   lo = __float2half_rn(x - __half2float(hi));
 }
-__device__ __forceinline__ void split2d(double x, __half& hi, __half& lo) {
-  hi = __double2half(x);
-  lo = __double2half(x - (double)__half2float(hi));
-}
 
 // exponent e with |x| * 2^-e < 2^14 for all |x| <= amax (0 when amax == 0)
 __device__ __forceinline__ int scale_exp(double amax) {
@@ -91,35 +87,49 @@ __device__ __forceinline__ int scale_exp(double amax) {
   return e - 14;
 }
 
-// per-projector and per-G maxima of |re|,|im| of anl[p][g]
+// x 2^-e rounded to FP32 from the FP64 bit pattern (no FP64 instruction:
+// GB300 runs FP64 at 1/72 of FP32); the power of two is applied after the
+// conversion for |e| < 100 (values that underflow FP32 then are below 2^-110
+// of the row maximum, far below the 22 bits the two pieces keep)
+__device__ __forceinline__ float f32_scaled(double x, int e) {
+  if (e > -100 && e < 100) return f32_from_f64_rn(x) * __uint_as_float((uint32_t)(127 - e) << 23);
+  return __double2float_rn(ldexp(x, -e));
+}
+
+// per-projector and per-G maxima of |re|,|im| of anl[p][g], compared as the
+// integer bit patterns with the sign cleared (no FP64 instruction)
 __global__ void k_anl_rowmax(const double2* __restrict__ anl, int nproj, int ngw,
                              double* __restrict__ pmax) {
-  __shared__ double red[256];
+  __shared__ unsigned long long red[256];
   const int p = blockIdx.x;
-  double m = 0.0;
+  const unsigned long long mask = 0x7FFFFFFFFFFFFFFFull;
+  unsigned long long m = 0;
   for (int g = threadIdx.x; g < ngw; g += blockDim.x) {
     const double2 a = anl[(size_t)p * ngw + g];
-    m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
+    m = max(m, max((unsigned long long)__double_as_longlong(a.x) & mask,
+                   (unsigned long long)__double_as_longlong(a.y) & mask));
   }
   red[threadIdx.x] = m;
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    if (threadIdx.x < s) red[threadIdx.x] = max(red[threadIdx.x], red[threadIdx.x + s]);
     __syncthreads();
   }
-  if (threadIdx.x == 0) pmax[p] = red[0];
+  if (threadIdx.x == 0) pmax[p] = __longlong_as_double((long long)red[0]);
 }
 
 __global__ void k_anl_colmax(const double2* __restrict__ anl, int nproj, int ngw,
                              double* __restrict__ gmax) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngw) return;
-  double m = 0.0;
+  const unsigned long long mask = 0x7FFFFFFFFFFFFFFFull;
+  unsigned long long m = 0;
   for (int p = 0; p < nproj; ++p) {
     const double2 a = anl[(size_t)p * ngw + g];
-    m = fmax(m, fmax(fabs(a.x), fabs(a.y)));
+    m = max(m, max((unsigned long long)__double_as_longlong(a.x) & mask,
+                   (unsigned long long)__double_as_longlong(a.y) & mask));
   }
-  gmax[g] = m;
+  gmax[g] = __longlong_as_double((long long)m);
 }
 
 // X1 pieces: rows 2p+c, K = 2ngw; element values of the interleaved form
@@ -135,15 +145,17 @@ __global__ void k_split_x1(const double2* __restrict__ anl, int nproj, int ngw,
   }
   if (g >= ngw) return;
   const double2 a = anl[(size_t)p * ngw + g];
-  const double re = ldexp(a.x, -e), im = ldexp(a.y, -e);
-  const double v[4] = {re, im, -im, re};  // (2p,2g) (2p,2g+1) (2p+1,2g) (2p+1,2g+1)
-  for (int q = 0; q < 4; ++q) {
-    const int r = 2 * p + (q >> 1), k = 2 * g + (q & 1);
-    __half hi, lo;
-    split2d(v[q], hi, lo);
-    X1[tc_index(0, r, k, nRT, nKS)] = hi;
-    X1[tc_index(1, r, k, nRT, nKS)] = lo;
-  }
+  const float re = f32_scaled(a.x, e), im = f32_scaled(a.y, e);
+  __half rh, rl, ih, il;
+  split2(re, rh, rl);
+  split2(im, ih, il);
+  // (2p,2g) = re, (2p,2g+1) = im, (2p+1,2g) = -im, (2p+1,2g+1) = re
+  *reinterpret_cast<__half2*>(X1 + tc_index(0, 2 * p, 2 * g, nRT, nKS)) = __halves2half2(rh, ih);
+  *reinterpret_cast<__half2*>(X1 + tc_index(1, 2 * p, 2 * g, nRT, nKS)) = __halves2half2(rl, il);
+  *reinterpret_cast<__half2*>(X1 + tc_index(0, 2 * p + 1, 2 * g, nRT, nKS)) =
+      __halves2half2(__hneg(ih), rh);
+  *reinterpret_cast<__half2*>(X1 + tc_index(1, 2 * p + 1, 2 * g, nRT, nKS)) =
+      __halves2half2(__hneg(il), rl);
 }
 
 // X2 = X1^T pieces: rows m = 2g+c, K = 2P, scaled per G
@@ -159,16 +171,19 @@ __global__ void k_split_x2(const double2* __restrict__ anl, int nproj, int ngw,
     rscale[2 * g + 1] = ldexpf(1.f, e);
   }
   const double2 a = anl[(size_t)p * ngw + g];
-  const double re = ldexp(a.x, -e), im = ldexp(a.y, -e);
+  const float re = f32_scaled(a.x, e), im = f32_scaled(a.y, e);
+  __half rh, rl, ih, il;
+  split2(re, rh, rl);
+  split2(im, ih, il);
   // X2[2g][2p]=re, X2[2g][2p+1]=-im, X2[2g+1][2p]=im, X2[2g+1][2p+1]=re
-  const double v[4] = {re, -im, im, re};
-  for (int q = 0; q < 4; ++q) {
-    const int r = 2 * g + (q >> 1), k = 2 * p + (q & 1);
-    __half hi, lo;
-    split2d(v[q], hi, lo);
-    X2[tc_index(0, r, k, nRT, nKS)] = hi;
-    X2[tc_index(1, r, k, nRT, nKS)] = lo;
-  }
+  *reinterpret_cast<__half2*>(X2 + tc_index(0, 2 * g, 2 * p, nRT, nKS)) =
+      __halves2half2(rh, __hneg(ih));
+  *reinterpret_cast<__half2*>(X2 + tc_index(1, 2 * g, 2 * p, nRT, nKS)) =
+      __halves2half2(rl, __hneg(il));
+  *reinterpret_cast<__half2*>(X2 + tc_index(0, 2 * g + 1, 2 * p, nRT, nKS)) =
+      __halves2half2(ih, rh);
+  *reinterpret_cast<__half2*>(X2 + tc_index(1, 2 * g + 1, 2 * p, nRT, nKS)) =
+      __halves2half2(il, rl);
 }
 
 // row maxima of |re|, |im| of x[n][0..ncols): blocks (chunk, row), the block

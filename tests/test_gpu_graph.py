@@ -73,6 +73,33 @@ def test_graph_replay_matches_individual_steps(cuda):
     g.close()
 
 
+def test_graph_cells_match_the_oracle(cuda):
+    """Two batched cells of different grids (FP64 form, fixed potential)
+    after two graph replays against the oracle's ETRS steps of each cell."""
+    from oracle import oracle as O
+    torch = _torch()
+    cells = []
+    for name in ("t12", "t12b"):
+        H, psi, occ = make(name, "fp64")
+        cells.append((name, H, dev(psi), occ, psi))
+    stream = torch.cuda.Stream()
+    g = Q.EtrsGraph([(H, p, occ) for _, H, p, occ, _ in cells], 0.05, stream=stream)
+    for _ in range(2):
+        g.launch(stream=stream)
+    g.check()
+    for name, H, p, occ, psi in cells:
+        cell = synth.make_cell(name)
+        oh = O.Ham(O.FT(O.Basis(H.basis.a, cell.ecut), *cell.grid), synth.vlocal(cell),
+                   synth.species(cell))
+        A = synth.kick()
+        oh.set_A(A)
+        ref = psi.T.copy()
+        for _ in range(2):
+            ref, _, _ = oh.etrs_step(ref, occ, 0.05, A, A, nthreads=8)
+        assert rel_err(p.cpu().numpy(), ref.T) < 1e-10, name
+    g.close()
+
+
 def test_graph_rejects_repeated_plan(cuda):
     H, psi, occ = make("t12", "fp64")
     p = dev(psi)
@@ -88,9 +115,39 @@ def test_autotune_keeps_hpsi(cuda):
     H.hpsi(p, before, occ)
     ch = H.autotune(p, occ)
     assert ch in (8, 16, 32, 64)
+    cfg = H.transform_config()
+    assert cfg["chunk"] == ch and cfg["radix_order"] in (0, 1, 2)
     after = torch.zeros_like(p)
     H.hpsi(p, after, occ)
     assert rel_err(after.cpu().numpy(), before.cpu().numpy()) < 1e-12
+
+
+@pytest.mark.parametrize("name,prec,tol", [("t12", "fp64", 1e-13), ("c1", "fp64", 1e-13),
+                                           ("c1", "mixed_df32", 1e-11), ("c1", "mixed", 1e-5)])
+def test_every_transform_shape_gives_the_same_hpsi(cuda, name, prec, tol):
+    """Every transform shape the autotuner can pick (radix order of the
+    Stockham passes, prime-factor splits, fused x-y-x kernel, register
+    lane-group y pass) gives the same H|psi> to the rounding of the form."""
+    torch = _torch()
+    H, psi, occ = make(name, prec)
+    p = dev(psi)
+    ref = torch.zeros_like(p)
+    H.hpsi(p, ref, occ)
+    r = ref.cpu().numpy()
+    seen = 0
+    for order in (0, 1, 2):
+        for pfa in (1, 0):
+            for fused in (1, 0):
+                for lane in (1, 0):
+                    if fused and not pfa:
+                        continue
+                    H.set_transform_config(order, pfa, fused, lane)
+                    assert H.transform_config()["radix_order"] == order
+                    out = torch.zeros_like(p)
+                    H.hpsi(p, out, occ)
+                    assert rel_err(out.cpu().numpy(), r) < tol, (order, pfa, fused, lane)
+                    seen += 1
+    assert seen == 18
 
 
 def test_bounded_wait_expires_and_context_survives(cuda):
