@@ -268,6 +268,14 @@ qbg_status qbg_update_vhxc(qbg_plan* plan, const double* rho, double* en,
  * qbg_set_density_basis and qbg_set_ionic_terms first. */
 qbg_status qbg_set_selfconsistent(qbg_plan* plan, int on);
 
+/* SlaterDet::gram (SlaterDet.cc:1043-1143, complex branch, norm-conserving):
+ * psi [ld x nst] FP64 is orthonormalised in place, C <- C L^{-H} with
+ * C^H C = L L^H.  The overlap C^H C and the product with L^{-H} (2 x 8 nst^2
+ * ngw flop) run on the device in FP64; the nst x nst Cholesky factor and its
+ * inverse are formed on the host.  QBG_ERR_DIVERGED when the overlap is not
+ * positive definite.  Synchronises the stream. */
+qbg_status qbg_gram(qbg_plan* plan, double* psi, int ld, int nst, void* stream);
+
 /* One ETRS step (ExponentialWavefunctionStepper::preupdate + update,
  * ExponentialWavefunctionStepper.cc:153-276; 4th-order Taylor
  * exponentials, ExponentialWavefunctionStepper.cc:51-148): psi [ld x nst]

@@ -115,6 +115,17 @@ def ref():
     return _ref
 
 
+def gram(c):
+    """SlaterDet::gram (SlaterDet.cc:1103-1135, complex branch): columns of c
+    [ngw x nst] orthonormalised as C L^{-H} with C^H C = L L^H (herk, potrf
+    lower, trsm right/lower/conjugate-transpose), in FP64."""
+    c = np.asarray(c, np.complex128)
+    s = c.conj().T @ c
+    L = np.linalg.cholesky(s)
+    # X L^H = C  ->  X = C L^{-H}
+    return np.linalg.solve(L.conj(), c.T).T
+
+
 def ref_species_load(path, rcps=1.0):
     """A pseudopotential read and initialised by the reference's own Species
     code (handle; ref_species_destroy frees it)."""

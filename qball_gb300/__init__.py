@@ -72,6 +72,7 @@ ABI = {
     "qbg_update_vhxc": [_P, _P, _P, _P],
     "qbg_set_selfconsistent": [_P, _I],
     "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
+    "qbg_gram": [_P, _P, _I, _I, _P],
     "qbg_etrs_adjoint_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P],
     "qbg_td_create": [_P, _I, _I, _P, _D, _I, _I, _P],
     "qbg_td_forward": [_P, _P, _P, _P, _P],
@@ -404,6 +405,12 @@ class Hamiltonian(FourierTransform):
         _check(lib().qbg_current(self.h, _dev_ptr(psi), ldv, n, _np_ptr(o), float(nel),
                                  _np_ptr(J), _stream_ptr(stream)), "qbg_current")
         return J
+
+    def gram(self, psi, nst=None, ld=None, stream=None):
+        """SlaterDet::gram: orthonormalise the device states psi in place."""
+        n = psi.shape[0] if nst is None else nst
+        ldv = psi.shape[-1] if ld is None else ld
+        _check(lib().qbg_gram(self.h, _dev_ptr(psi), ldv, n, _stream_ptr(stream)), "qbg_gram")
 
     def etrs_step(self, psi, occ, dt, A_t=None, A_tdt=None, rho=None, want_nel=False,
                   nst=None, ld=None, stream=None):

@@ -256,6 +256,12 @@ qbg_status ensure_nl(qbg_plan* p, cudaStream_t st);
 qbg_status exponential(qbg_plan* p, double2* psi, int ld, int nst, const double* d_occ,
                        double dt1, cudaStream_t st);
 
+// Gram orthonormalisation products (qbg_nl.cu), FP64 on the device
+qbg_status gram_overlap(qbg_plan* p, const double2* psi, int ld, int nst, double2* S,
+                        cudaStream_t st);
+qbg_status gram_apply(qbg_plan* p, const double2* psi, int ld, int nst, const double2* T,
+                      double2* out, int ldo, cudaStream_t st);
+
 // adjoint support (qbg_nl.cu, qbg_tc.cu)
 qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_t st);
 qbg_status nl_project64(qbg_plan* p, const double2* table, const double2* x, int ld, int nst,

@@ -268,11 +268,12 @@ qbg_status nl_build(qbg_plan* p, cudaStream_t st) {
 constexpr int GT = 64;   // output tile edge
 constexpr int GK = 16;   // k step
 
-// part[z][n][p] = sum_{g in split z} conj(anl[p][g]) psi[n][g]
+// part[z][n][p] = sum_{g in split z} conj(anl[p][g]) psi[n][g], g < ngw;
+// anl rows lda apart
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_fnl(const cplx<T>* __restrict__ anl, int ngw, int nproj, const cplx<T>* __restrict__ psi,
-      int ld, int nst, double2* __restrict__ part, int kchunk) {
+k_fnl(const cplx<T>* __restrict__ anl, int lda, int ngw, int nproj,
+      const cplx<T>* __restrict__ psi, int ld, int nst, double2* __restrict__ part, int kchunk) {
   using C = cplx<T>;
   __shared__ C As[GK][GT];
   __shared__ C Bs[GK][GT];
@@ -291,7 +292,7 @@ k_fnl(const cplx<T>* __restrict__ anl, int ngw, int nproj, const cplx<T>* __rest
       const int k = k0 + kk;
       C a, b;
       a.x = a.y = b.x = b.y = T(0);
-      if (k < ke && p0 + r < nproj) a = anl[(size_t)(p0 + r) * ngw + k];
+      if (k < ke && p0 + r < nproj) a = anl[(size_t)(p0 + r) * lda + k];
       if (k < ke && n0 + r < nst) b = psi[(size_t)(n0 + r) * ld + k];
       As[kk][r] = a;
       Bs[kk][r] = b;
@@ -359,11 +360,11 @@ k_fnl_reduce(const double2* __restrict__ part, int nsplit, int nproj, int nst,
   if (threadIdx.x == 0 && enl_part) enl_part[blockIdx.x] = red[0];
 }
 
-// out[n][g] = sum_p anl[p][g] fnl[n][p]
+// out[n][g] = sum_p anl[p][g] fnl[n][p], g < ngw; anl rows lda apart
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_nl_hpsi(const cplx<T>* __restrict__ anl, int ngw, int nproj, const cplx<T>* __restrict__ fnl,
-          int nst, cplx<T>* __restrict__ out, int ldo) {
+k_nl_hpsi(const cplx<T>* __restrict__ anl, int lda, int ngw, int nproj,
+          const cplx<T>* __restrict__ fnl, int nst, cplx<T>* __restrict__ out, int ldo) {
   using C = cplx<T>;
   __shared__ C As[GK][GT];
   __shared__ C Bs[GK][GT];
@@ -382,7 +383,7 @@ k_nl_hpsi(const cplx<T>* __restrict__ anl, int ngw, int nproj, const cplx<T>* __
         const int kk = e >> 6, gg = e & 63;
         C a;
         a.x = a.y = T(0);
-        if (k0 + kk < nproj && g0 + gg < ngw) a = anl[(size_t)(k0 + kk) * ngw + g0 + gg];
+        if (k0 + kk < nproj && g0 + gg < ngw) a = anl[(size_t)(k0 + kk) * lda + g0 + gg];
         As[kk][gg] = a;
       }
       {
@@ -451,7 +452,7 @@ qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int n
   if (s) return s;
   {
     PhaseTimer pt(p, PH_FNL_GEMM, st);
-    k_fnl<T><<<dim3(mt, nt, split), 256, 0, st>>>(anl, p->ngw, P, psi, ld, nst,
+    k_fnl<T><<<dim3(mt, nt, split), 256, 0, st>>>(anl, p->ngw, p->ngw, P, psi, ld, nst,
                                                    (double2*)p->d_fpart, kchunk);
     QBG_LAUNCHED(p);
   }
@@ -469,7 +470,7 @@ qbg_status nl_apply(qbg_plan* p, const cplx<T>* psi, int ld, cplx<T>* out, int n
   {
     PhaseTimer pt(p, PH_ENL_HPSI, st);
     k_nl_hpsi<T><<<dim3((p->ngw + GT - 1) / GT, nt), 256, 0, st>>>(
-        anl, p->ngw, P, (const cplx<T>*)p->d_fnl, nst, out, ld);
+        anl, p->ngw, p->ngw, P, (const cplx<T>*)p->d_fnl, nst, out, ld);
     QBG_LAUNCHED(p);
   }
   return QBG_OK;
@@ -586,12 +587,45 @@ qbg_status nl_project64(qbg_plan* p, const double2* table, const double2* x, int
   split = (p->ngw + kchunk - 1) / kchunk;
   const qbg_status s = ensure(&p->d_fpart, &p->fpart_bytes, (size_t)split * P * nst * sizeof(double2));
   if (s != QBG_OK) return s;
-  k_fnl<double><<<dim3(mt, nt, split), 256, 0, st>>>(table, p->ngw, P, x, ld, nst,
+  k_fnl<double><<<dim3(mt, nt, split), 256, 0, st>>>(table, p->ngw, p->ngw, P, x, ld, nst,
                                                       (double2*)p->d_fpart, kchunk);
   QBG_LAUNCHED(p);
   const size_t total = (size_t)P * nst;
   k_part_sum<<<(unsigned)((total + 255) / 256), 256, 0, st>>>((const double2*)p->d_fpart, split,
                                                               total, f);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+// ---------------------------------------------- Gram (SlaterDet::gram)
+// S[n][m] = <psi_m|psi_n> = sum_g conj(psi[m][g]) psi[n][g] (FP64, device)
+qbg_status gram_overlap(qbg_plan* p, const double2* psi, int ld, int nst, double2* S,
+                        cudaStream_t st) {
+  const int mt = (nst + GT - 1) / GT;
+  int split = std::max(1, (4 * 152 + mt * mt - 1) / (mt * mt));
+  split = std::min(split, std::max(1, p->ngw / GK));
+  int kchunk = (p->ngw + split - 1) / split;
+  kchunk = (kchunk + GK - 1) / GK * GK;
+  split = (p->ngw + kchunk - 1) / kchunk;
+  const qbg_status s =
+      ensure(&p->d_fpart, &p->fpart_bytes, (size_t)split * nst * nst * sizeof(double2));
+  if (s != QBG_OK) return s;
+  k_fnl<double><<<dim3(mt, mt, split), 256, 0, st>>>(psi, ld, p->ngw, nst, psi, ld, nst,
+                                                      (double2*)p->d_fpart, kchunk);
+  QBG_LAUNCHED(p);
+  const size_t total = (size_t)nst * nst;
+  k_part_sum<<<(unsigned)((total + 255) / 256), 256, 0, st>>>((const double2*)p->d_fpart, split,
+                                                              total, S);
+  QBG_LAUNCHED(p);
+  return QBG_OK;
+}
+
+// out[n][g] = sum_m psi[m][g] T[n][m] (FP64, device)
+qbg_status gram_apply(qbg_plan* p, const double2* psi, int ld, int nst, const double2* T,
+                      double2* out, int ldo, cudaStream_t st) {
+  const int nt = (nst + GT - 1) / GT;
+  k_nl_hpsi<double><<<dim3((p->ngw + GT - 1) / GT, nt), 256, 0, st>>>(psi, ld, p->ngw, nst, T,
+                                                                       nst, out, ldo);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }

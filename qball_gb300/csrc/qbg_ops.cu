@@ -2,6 +2,7 @@
 // density, current and the ETRS step.
 #include <algorithm>
 #include <cmath>
+#include <complex>
 #include <vector>
 
 #include "qbg_internal.h"
@@ -444,6 +445,71 @@ qbg_status qbg_current(qbg_plan* p, const double* psi, int ld, int nst, const do
       for (int d = 0; d < 3; ++d) s[d] += p->h_red[3 * b + d];
   }
   for (int d = 0; d < 3; ++d) J[d] = -s[d] + p->A[d] * nel;
+  return QBG_OK;
+}
+
+// SlaterDet::gram (SlaterDet.cc:1043-1143), complex branch, norm-conserving:
+// S = C^H C (herk), S = L L^H (potrf, lower), C <- C L^{-H} (trsm).  The two
+// nst^2 ngw products run on the device in FP64; the nst^3 Cholesky factor
+// and the triangular inverse are formed on the host (a 432-state overlap is
+// 3 MB) in FP64, in the column order of the LAPACK algorithms.
+qbg_status qbg_gram(qbg_plan* p, double* psi_, int ld, int nst, void* stream) {
+  QBG_TRY(check_common(p, psi_, ld, nst, "qbg_gram"));
+  if (nst == 0) return QBG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  double2* psi = (double2*)psi_;
+  const size_t nn = (size_t)nst * nst;
+  QBG_TRY(ensure(&p->d_w[2], &p->w_bytes[2], sizeof(double2) * std::max(nn, (size_t)ld * nst)));
+  double2* S = (double2*)p->d_w[2];
+  QBG_TRY(gram_overlap(p, psi, ld, nst, S, st));
+  std::vector<std::complex<double>> h(nn);
+  QBG_CUDA(cudaMemcpyAsync(h.data(), S, sizeof(double2) * nn, cudaMemcpyDeviceToHost, st));
+  QBG_CUDA(cudaStreamSynchronize(st));
+  // A(i, j) = <psi_i|psi_j> = h[j*nst + i]; lower Cholesky A = L L^H in place
+  auto A = [&](int i, int j) -> std::complex<double>& { return h[(size_t)j * nst + i]; };
+  for (int j = 0; j < nst; ++j) {
+    double d = A(j, j).real();
+    for (int k = 0; k < j; ++k) d -= std::norm(A(j, k));
+    if (!(d > 0.0)) {
+      set_error("qbg_gram: the overlap matrix is not positive definite at state %d "
+                "(linearly dependent states)", j);
+      return QBG_ERR_DIVERGED;
+    }
+    const double ljj = std::sqrt(d);
+    A(j, j) = ljj;
+    for (int i = j + 1; i < nst; ++i) {
+      std::complex<double> t = A(i, j);
+      for (int k = 0; k < j; ++k) t -= A(i, k) * std::conj(A(j, k));
+      A(i, j) = t / ljj;
+    }
+  }
+  // U = L^{-H} (upper triangular); psi'_n = sum_m psi_m U(m, n); the device
+  // product wants T[n][m] = U(m, n)
+  std::vector<std::complex<double>> Li(nn, 0.0);  // L^{-1}, lower
+  for (int j = 0; j < nst; ++j) {
+    Li[(size_t)j * nst + j] = 1.0 / A(j, j);
+    for (int i = j + 1; i < nst; ++i) {
+      std::complex<double> t = 0.0;
+      for (int k = j; k < i; ++k) t -= A(i, k) * Li[(size_t)j * nst + k];
+      Li[(size_t)j * nst + i] = t / A(i, i);
+    }
+  }
+  std::vector<double2> T(nn, make_double2(0.0, 0.0));
+  for (int n = 0; n < nst; ++n)
+    for (int m = 0; m <= n; ++m) {
+      // U(m, n) = conj(Linv(n, m))
+      const std::complex<double> u = std::conj(Li[(size_t)m * nst + n]);
+      T[(size_t)n * nst + m] = make_double2(u.real(), u.imag());
+    }
+  QBG_TRY(ensure(&p->d_w[3], &p->w_bytes[3], sizeof(double2) * nn));
+  double2* dT = (double2*)p->d_w[3];
+  p->occ_cache.clear();  // d_w[3] held the per-state factors
+  QBG_CUDA(cudaMemcpyAsync(dT, T.data(), sizeof(double2) * nn, cudaMemcpyHostToDevice, st));
+  double2* out = (double2*)p->d_w[2];
+  QBG_TRY(gram_apply(p, psi, ld, nst, dT, out, ld, st));
+  QBG_CUDA(cudaMemcpy2DAsync(psi, sizeof(double2) * ld, out, sizeof(double2) * ld,
+                             sizeof(double2) * p->ngw, nst, cudaMemcpyDeviceToDevice, st));
+  QBG_CUDA(cudaStreamSynchronize(st));  // T is a host stack buffer
   return QBG_OK;
 }
 

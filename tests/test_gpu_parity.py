@@ -392,3 +392,30 @@ def test_hpsi_and_etrs_real_pseudopotential_tables(cuda, prec, gemm, tol):
     H.etrs_step(p, occ, 0.05)
     ref2, _, _ = oh.etrs_step(psi.T.copy(), occ, 0.05, A, A, nthreads=NT)
     assert rel_err(p.cpu().numpy(), ref2.T) < (tol if prec == "fp64" else 5e-5)
+
+
+@pytest.mark.parametrize("name,kw", [("c1", {}), ("c2", dict(natoms=8, nst=40))])
+def test_gram_vs_oracle(cuda, name, kw):
+    """SlaterDet::gram on the device (FP64 overlap and product, host
+    Cholesky) against the oracle's restatement on the same seeded
+    non-orthogonal states, with a padded leading dimension."""
+    cell = synth.make_cell(name, **kw)
+    b = Q.Basis(cell.L, cell.ecut)
+    H = Q.Hamiltonian(b, *cell.grid)
+    rng = np.random.default_rng(3)
+    n = cell.nst
+    c = (rng.standard_normal((n, b.ngw)) + 1j * rng.standard_normal((n, b.ngw))) \
+        * np.exp(-b.kpg2 / 8)[None, :]
+    ld = b.ngw + 5
+    cp = np.zeros((n, ld), complex)
+    cp[:, :b.ngw] = c
+    cp[:, b.ngw:] = 9.0
+    torch = _torch()
+    p = dev(cp)
+    H.gram(p, ld=ld)
+    out = p.cpu().numpy()
+    ref = O.gram(c.T).T
+    assert rel_err(out[:, :b.ngw], ref) < 1e-12
+    ov = out[:, :b.ngw].conj() @ out[:, :b.ngw].T
+    assert np.abs(ov - np.eye(n)).max() < 1e-12
+    assert np.all(out[:, b.ngw:] == 9.0)

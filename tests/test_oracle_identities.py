@@ -84,3 +84,20 @@ def test_etrs_small_dt_matches_exact_propagator(small):
     e = 0.5 * ((kx[0] - A[0]) ** 2 + (kx[1] - A[1]) ** 2 + (kx[2] - A[2]) ** 2)
     exact = np.exp(-1j * e * dt)[:, None] * psi.T
     assert np.abs(out - exact).max() < 1e-9
+
+
+def test_oracle_gram_orthonormalises_like_the_reference():
+    """The oracle's SlaterDet::gram (C L^{-H}, C^H C = L L^H): orthonormal
+    columns spanning the same space, L^H upper triangular (the first column
+    only rescaled), and equal to the Cholesky row form of the seeded-state
+    generator."""
+    from oracle import oracle as O
+    from qball_gb300 import synth
+    rng = np.random.default_rng(4)
+    c = rng.standard_normal((300, 12)) + 1j * rng.standard_normal((300, 12))
+    x = O.gram(c)
+    assert np.abs(x.conj().T @ x - np.eye(12)).max() < 1e-13
+    t = np.linalg.lstsq(c, x, rcond=None)[0]  # x = c t, t upper triangular
+    assert np.abs(np.tril(t, -1)).max() < 1e-12
+    assert np.allclose(x[:, 0], c[:, 0] / np.linalg.norm(c[:, 0]), atol=1e-14)
+    assert np.abs(x.T - synth.gram(c.T)).max() < 1e-13

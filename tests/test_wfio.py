@@ -91,3 +91,23 @@ def test_missing_and_short_files(states, workdir):
         wfio.read_states(base, 1, N, ft.forward)
     with pytest.raises(ValueError):
         wfio.write_states(base, c[:1], ft.backward, eig=[0.0])
+
+
+@pytest.mark.gpu
+def test_device_transforms_write_the_oracles_files(cuda, workdir, states):
+    """The checkpoint files written through the C ABI's FP64 transforms (a
+    plan on the basis' own grid) hold the oracle's psi(r) to 1e-13 and read
+    back through the device forward transform to the coefficients."""
+    import qball_gb300 as Q
+    cell, a, b, ft, c = states
+    qb = Q.Basis(a, cell.ecut)
+    bwd, fwd = wfio.device_transforms(qb)
+    base = os.path.join(workdir, "wf")
+    wfio.write_states(base, c, bwd)
+    n012 = int(np.prod(b.np))
+    for n in range(c.shape[0]):
+        f = np.fromfile(wfio.state_file(base, n), dtype=np.complex128)
+        ref = ft.backward(c[n])
+        assert np.linalg.norm(f - ref) <= 1e-13 * np.linalg.norm(ref)
+    back = wfio.read_states(base, c.shape[0], n012, fwd)
+    assert np.abs(back - c).max() < 1e-13
