@@ -273,6 +273,12 @@ class FourierTransform:
         _check(lib().qbg_launch_count(self.h, ctypes.byref(c)), "qbg_launch_count")
         return c.value
 
+    def gram(self, psi, nst=None, ld=None, stream=None):
+        """SlaterDet::gram: orthonormalise the device states psi in place."""
+        n = psi.shape[0] if nst is None else nst
+        ldv = psi.shape[-1] if ld is None else ld
+        _check(lib().qbg_gram(self.h, _dev_ptr(psi), ldv, n, _stream_ptr(stream)), "qbg_gram")
+
     # ---- FourierTransform::backward / forward, batched over states
     def backward(self, c, f, nbatch=None, ldc=None, stream=None):
         nb = c.shape[0] if nbatch is None else nbatch
@@ -405,12 +411,6 @@ class Hamiltonian(FourierTransform):
         _check(lib().qbg_current(self.h, _dev_ptr(psi), ldv, n, _np_ptr(o), float(nel),
                                  _np_ptr(J), _stream_ptr(stream)), "qbg_current")
         return J
-
-    def gram(self, psi, nst=None, ld=None, stream=None):
-        """SlaterDet::gram: orthonormalise the device states psi in place."""
-        n = psi.shape[0] if nst is None else nst
-        ldv = psi.shape[-1] if ld is None else ld
-        _check(lib().qbg_gram(self.h, _dev_ptr(psi), ldv, n, _stream_ptr(stream)), "qbg_gram")
 
     def etrs_step(self, psi, occ, dt, A_t=None, A_tdt=None, rho=None, want_nel=False,
                   nst=None, ld=None, stream=None):

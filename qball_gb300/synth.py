@@ -206,10 +206,11 @@ def enable_selfconsistent(H, cell, p, occ):
 
 
 def device_wavefunctions(cell, basis, nst=None):
-    """Seeded random states on cuda, Gram-orthonormalised in FP64: the
-    nst x nst Cholesky factor on the host, the products on the device
-    (torch complex128 [nst, ngw])."""
+    """Seeded random states on cuda, Gram-orthonormalised in FP64 by the
+    library's SlaterDet::gram (qbg_gram: products on the device, the nst x nst
+    Cholesky factor on the host); torch complex128 [nst, ngw]."""
     import torch
+    import qball_gb300 as Q
     rng = np.random.default_rng(cell.seed + 7)
     n, ngw = (cell.nst if nst is None else nst), basis.ngw
     env = torch.from_numpy(np.exp(-basis.kpg2 / 8.0)).cuda()
@@ -218,8 +219,5 @@ def device_wavefunctions(cell, basis, nst=None):
         s1 = min(n, s0 + 64)
         blk = rng.standard_normal((s1 - s0, ngw)) + 1j * rng.standard_normal((s1 - s0, ngw))
         c[s0:s1] = torch.from_numpy(blk).cuda() * env
-    # c <- conj(L)^-1 c with S = L L^H
-    S = (c.conj() @ c.T).cpu().numpy()
-    L = np.linalg.cholesky(S)
-    Linv = np.linalg.inv(np.conj(L))
-    return torch.from_numpy(Linv).cuda() @ c
+    Q.FourierTransform(basis, *cell.grid).gram(c)
+    return c
