@@ -286,8 +286,27 @@ def nproj_of(cell):
     return cell.natoms * (cell.lmax + 1) ** 2
 
 
+def phase_bytes(H, cell, basis):
+    """Algorithmic HBM bytes per STATE of each transform phase of one H|psi>
+    (the z-column intermediate in and out, psi in, H psi out, the v(r) tile
+    once per launch group of H.chunk states)."""
+    n0, n1, n2 = cell.grid
+    ngw, nrods = basis.ngw, basis.nrods
+    cs = 8 if H.precision in ("mixed", "mixed_nl64") else 16  # complex transform element
+    vs = {"mixed_df32": 8, "mixed": 4, "mixed_nl64": 4}.get(H.precision, 8)
+    zrows = cs * n2 * nrods
+    N = n0 * n1 * n2
+    return {"ft_z_bwd": 16 * ngw + zrows,
+            "ft_z_fwd": zrows + 2 * 16 * ngw,
+            "ft_xyx_vloc": 2 * zrows + N * vs / max(1, H.chunk),
+            "ft_y_density": zrows + N * 8 / max(1, H.chunk)}
+
+
 def roofline_of(H, cell, basis, prof, peaks, nst):
-    """The dominant phase of one H application (largest device time)."""
+    """The dominant phase of one H application (largest device time), against
+    the bound the roofline contract names: the tensor pipe for the GEMMs, HBM
+    for everything else (with the compute pipe that actually bounds a
+    transform beside it as compute_view)."""
     model = phase_model(H, cell, basis)
     dom = max((k for k in model if k in prof and prof[k][1]), key=lambda k: prof[k][0])
     tot_ms, nl = prof[dom]
@@ -317,12 +336,26 @@ def roofline_of(H, cell, basis, prof, peaks, nst):
                     "frac": hbm_gbs / hbm_peak,
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks
                     else "fallback 6785.5 GB/s"}
-    return {"kernel": dom, "bound": bound, "achieved": achieved, "peak": peak,
-            "hbm_view": hbm_view,
-            "unit": unit, "frac": achieved / peak, "traffic": traffic,
+    compute = {"pipe": bound, "achieved": achieved, "peak": peak, "unit": unit,
+               "frac": achieved / peak,
+               "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 kind::f16 runs at the "
+                               "same rate)" if bound == "tensor"
+                               else "profiles/peaks_gb300.json")}
+    if bound == "tensor":
+        head = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "peak_source": compute["peak_source"]}
+    else:
+        # algorithmic bytes per launch over the live per-launch time
+        hbm_peak = float(peaks.get("hbm_gbs", 6785.5))
+        alg = phase_bytes(H, cell, basis).get(dom, 0.0) * nst / max(nl, 1)
+        gbs = alg / (per_launch_ms / 1000.0) / 1e9
+        head = {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": gbs / hbm_peak, "algorithmic_bytes_per_launch": alg,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks
+                else "fallback 6785.5 GB/s"}
+    return {"kernel": dom, **head, "traffic": traffic, "compute_view": compute,
+            "hbm_view_measured_traffic": hbm_view,
             "per_launch_ms": per_launch_ms, "launches_per_H": nl,
-            "peak_source": ("MEASURED_PEAKS.json bf16_tflops (FP16 kind::f16 runs at the same "
-                            "rate)" if bound == "tensor" else "profiles/peaks_gb300.json"),
             "phases_ms_per_H": {k: round(v[0], 3) for k, v in prof.items() if v[1]},
             "phase_frac_of_peak": {k: round(model[k][0] * nst / (v[0] / 1000.0) / 1e12 /
                                             (float(peaks.get("bf16_tflops", 1917.4))
