@@ -103,6 +103,22 @@ def main():
         e1.record(stream)
         stream.synchronize()
         ms_seq = e0.elapsed_time(e1)
+    # device time of one step of every cell with each kernel run alone (the
+    # plan's per-phase profiler): what the graph would take with no launch
+    # cost and no overlap between cells
+    busy_ms = 0.0
+    for H, p, occ in seq:
+        H.profile(True)
+        H.etrs_step(p.clone(), occ, args.dt, stream=stream)
+        busy_ms += sum(v[0] for v in H.profile_read().values())
+        H.profile(False)
+    stream.synchronize()
+    launches_per_step = 0
+    for H, p, occ in seq:
+        l0 = H.launches()
+        H.etrs_step(p.clone(), occ, args.dt, stream=stream)
+        launches_per_step += H.launches() - l0
+    stream.synchronize()
     graph = Q.EtrsGraph(bat, args.dt, stream=stream)
     for _ in range(args.warmup):
         graph.launch(stream=stream)
@@ -129,6 +145,9 @@ def main():
         "cell_steps_per_s_graph": n * args.steps / (ms_graph / 1000.0),
         "cell_steps_per_s_sequential": n * args.steps / (ms_seq / 1000.0),
         "graph_speedup": ms_seq / ms_graph,
+        "ms_per_step_graph": ms_graph / args.steps,
+        "kernel_device_ms_per_step": busy_ms,
+        "kernel_launches_per_step": launches_per_step,
         "max_rel_diff_graph_vs_sequential": diff,
         "chunks": sorted({H.chunk for H, _, _ in bat}),
         "transform_shapes": _shape_counts([H.transform_config() for H, _, _ in bat]),
