@@ -80,6 +80,8 @@ def parse():
     ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--cpu-states", type=int, default=16)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--fp64-slices", type=int, default=7, choices=[6, 7],
+                    help="7-bit slices per operand of the FP64 form's tensor-core GEMMs")
     ap.add_argument("--fp64-simt-steps", type=int, default=0,
                     help="ETRS steps of the FP64 form with FP64-FMA projector GEMMs (0: one "
                          "profiled H|psi> only; a step takes ~40 s on the 216-atom cell)")
@@ -569,7 +571,7 @@ def run_ours(args, rank, world, local):
     for label, form, gemm, steps, warm in runs:
         _, _, H2, _ = make_system(args.config, form, psi_np=psi)
         if gemm:
-            H2.set_fp64_gemm(gemm)
+            H2.set_fp64_gemm(gemm, args.fp64_slices)
         H2.set_vector_potential(A)
         if hxc:
             synth.enable_selfconsistent(H2, cell, psi, occ)
