@@ -268,6 +268,20 @@ qbg_status qbg_update_vhxc(qbg_plan* plan, const double* rho, double* en,
  * qbg_set_density_basis and qbg_set_ionic_terms first. */
 qbg_status qbg_set_selfconsistent(qbg_plan* plan, int on);
 
+/* on != 0: approximated ETRS, the stepper's AETRS option (ExponentialWave-
+ * functionStepper with approximated_, ExponentialWavefunctionStepper.cc:
+ * 153-276; SelfConsistentPotential::extrapolate, SelfConsistentPotential.cc:
+ * 46-73).  Every qbg_etrs_step stores the local potential of H(t) (after the
+ * self-consistent rebuild when that is on); from the third stored step on,
+ * psi(t) is propagated half a step with H(t), then half a step with the
+ * potential extrapolated as 3 v(t) - 3 v(t-dt) + v(t-2dt) and the vector
+ * potential A_t (the reference's preupdate runs before the vector potential
+ * moves on), and no predicted state or density is formed: 8 H|psi> per step
+ * instead of 12, and one density (the loop top's) instead of two.  rho_mid and
+ * nel then receive the density of psi(t+dt).  Switching resets the stored
+ * potentials. */
+qbg_status qbg_set_aetrs(qbg_plan* plan, int on);
+
 /* SlaterDet::gram (SlaterDet.cc:1043-1143, complex branch, norm-conserving):
  * psi [ld x nst] FP64 is orthonormalised in place, C <- C L^{-H} with
  * C^H C = L L^H.  The overlap C^H C and the product with L^{-H} (2 x 8 nst^2

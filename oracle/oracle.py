@@ -81,6 +81,9 @@ def lib():
                                         _P, _I]
         L.qbo_etrs_step_hxc.restype = _D
         L.qbo_ham_get_vr.argtypes = [_P, _P]
+        L.qbo_aetrs_step.argtypes = [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _I, _P, _P, _P,
+                                     _P, _I]
+        L.qbo_aetrs_step.restype = _D
     return _lib
 
 
@@ -360,6 +363,34 @@ class Ham:
         nel = lib().qbo_etrs_step(self.h, _ptr(psi), ngw, nst, _ptr(occ), float(dt),
                                   _ptr(A_t), _ptr(A_tdt), _ptr(rho), nthreads)
         return psi, rho, nel
+
+    def aetrs_step(self, psi, occ, dt, A_t, A_tdt, hxc=None, nthreads=1):
+        """AETRS step (approximated_ stepper); the stored potentials live on
+        this object (reset_aetrs clears them).  hxc: an Hxc object for the
+        self-consistent loop top, or None for a fixed potential."""
+        n012 = self.ft.n012
+        if getattr(self, "_vhist", None) is None:
+            self.reset_aetrs()
+        psi = np.asfortranarray(psi, dtype=np.complex128).copy(order="F")
+        ngw, nst = psi.shape
+        occ = np.ascontiguousarray(occ, dtype=np.float64)
+        A_t = np.ascontiguousarray(A_t, dtype=np.float64)
+        A_tdt = np.ascontiguousarray(A_tdt, dtype=np.float64)
+        st = ctypes.c_int(self._stored)
+        if hxc is None:
+            args = (None, None, 0, None, None)
+        else:
+            args = (hxc.vft.h, _ptr(hxc.vbasis.kpg2), hxc.vbasis.ngw, _ptr(hxc.vion),
+                    _ptr(hxc.rhopst))
+        lib().qbo_aetrs_step(self.h, _ptr(psi), ngw, nst, _ptr(occ), float(dt), _ptr(A_t),
+                             _ptr(A_tdt), *args, _ptr(self._vhist), ctypes.byref(st), nthreads)
+        self._stored = st.value
+        assert n012 == self._vhist.size // 3
+        return psi
+
+    def reset_aetrs(self):
+        self._vhist = np.zeros(3 * self.ft.n012)
+        self._stored = 0
 
     def etrs_step_hxc(self, psi, occ, dt, A_t, A_tdt, hxc, want_rho=False, nthreads=1):
         """ETRS step with v_r rebuilt by update_vhxc (hxc: an Hxc object)."""

@@ -1034,6 +1034,60 @@ double qbo_update_vhxc(const qbo_ft* vft, const double* g2, int ngv,
   return ehart;
 }
 
+/* AETRS, ExponentialWavefunctionStepper with approximated_ (Exponential-
+ * WavefunctionStepper.cc:153-276, SelfConsistentPotential.cc:46-73) on top of
+ * the self-consistent loop top (vft != NULL) or a fixed potential (vft ==
+ * NULL): vhist [3][n012] holds v_r of the last three steps, *stored counts
+ * them.  From the third stored step on the step is two half-step
+ * exponentials, the second with v = 3 v2 - 3 v1 + 1 v0 and A_t; before that
+ * it is the ETRS step.  The predicted state the reference also computes in
+ * that case is overwritten there unused (:218-225), so it is not formed
+ * here. */
+double qbo_aetrs_step(qbo_ham* h, double* psi, int ld, int nst, const double* occ,
+                      double dt, const double* A_t, const double* A_tdt,
+                      const qbo_ft* vft, const double* g2, int ngv,
+                      const double* vion_g, const double* rhopst_g, double* vhist,
+                      int* stored, int nthreads) {
+  const long n012 = (long)h->ft->np0 * h->ft->np1 * h->ft->np2;
+  const size_t len = 2 * (size_t)ld * nst;
+  double* rho = (double*)malloc(sizeof(double) * (size_t)n012);
+  double* dwf = (double*)malloc(sizeof(double) * len);
+  double* expwf = (double*)malloc(sizeof(double) * len);
+  double* newwf = (double*)malloc(sizeof(double) * len);
+  const double dt1 = 0.5 * dt;
+  if (vft) {
+    qbo_update_density(h->ft, psi, ld, nst, occ, h->omega, rho, nthreads);
+    qbo_update_vhxc(vft, g2, ngv, vion_g, rhopst_g, rho, h->omega, h->v_r, NULL);
+  }
+  /* potential_[0] = potential_[1]; [1] = [2]; [2] = current */
+  memcpy(vhist, vhist + n012, sizeof(double) * (size_t)n012);
+  memcpy(vhist + n012, vhist + 2 * n012, sizeof(double) * (size_t)n012);
+  memcpy(vhist + 2 * n012, h->v_r, sizeof(double) * (size_t)n012);
+  if (*stored < 3) ++*stored;
+  qbo_ham_set_A(h, A_t);
+  qbo_exponential(h, psi, ld, nst, occ, dt1, dwf, expwf, nthreads);
+  double nel = 0.0;
+  if (*stored >= 3) {
+    for (long i = 0; i < n012; ++i)
+      h->v_r[i] = 3.0 * vhist[2 * n012 + i] - 3.0 * vhist[n012 + i] + 1.0 * vhist[i];
+    qbo_exponential(h, psi, ld, nst, occ, dt1, dwf, expwf, nthreads);
+    qbo_ham_set_A(h, A_tdt);
+  } else {
+    memcpy(newwf, psi, sizeof(double) * len);
+    qbo_exponential(h, psi, ld, nst, occ, dt1, dwf, expwf, nthreads);
+    nel = qbo_update_density(h->ft, psi, ld, nst, occ, h->omega, rho, nthreads);
+    if (vft) qbo_update_vhxc(vft, g2, ngv, vion_g, rhopst_g, rho, h->omega, h->v_r, NULL);
+    qbo_ham_set_A(h, A_tdt);
+    memcpy(psi, newwf, sizeof(double) * len);
+    qbo_exponential(h, psi, ld, nst, occ, dt1, dwf, expwf, nthreads);
+  }
+  free(rho);
+  free(dwf);
+  free(expwf);
+  free(newwf);
+  return nel;
+}
+
 double qbo_etrs_step_hxc(qbo_ham* h, double* psi, int ld, int nst,
                          const double* occ, double dt, const double* A_t,
                          const double* A_tdt, const qbo_ft* vft,

@@ -136,6 +136,11 @@ double qbo_etrs_step_hxc(qbo_ham* h, double* psi, int ld, int nst,
                          const double* rhopst_g, double* rho_mid, int nthreads);
 
 void qbo_ham_get_vr(const qbo_ham* h, double* v);
+double qbo_aetrs_step(qbo_ham* h, double* psi, int ld, int nst, const double* occ,
+                      double dt, const double* A_t, const double* A_tdt,
+                      const qbo_ft* vft, const double* g2, int ngv,
+                      const double* vion_g, const double* rhopst_g, double* vhist,
+                      int* stored, int nthreads);
 
 #ifdef __cplusplus
 }

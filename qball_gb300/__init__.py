@@ -73,6 +73,7 @@ ABI = {
     "qbg_set_selfconsistent": [_P, _I],
     "qbg_etrs_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P],
     "qbg_gram": [_P, _P, _I, _I, _P],
+    "qbg_set_aetrs": [_P, _I],
     "qbg_etrs_adjoint_step": [_P, _P, _I, _I, _P, _D, _P, _P, _P, _P, _P, _P, _P],
     "qbg_td_create": [_P, _I, _I, _P, _D, _I, _I, _P],
     "qbg_td_forward": [_P, _P, _P, _P, _P],
@@ -375,6 +376,10 @@ class Hamiltonian(FourierTransform):
         _check(lib().qbg_update_vhxc(self.h, _dev_ptr(rho), _np_ptr(en) if want_energies else None,
                                      _stream_ptr(stream)), "qbg_update_vhxc")
         return dict(zip(("ehart", "exc", "eps"), en.tolist())) if want_energies else None
+
+    def set_aetrs(self, on=True):
+        """Approximated ETRS (the reference stepper's AETRS option)."""
+        _check(lib().qbg_set_aetrs(self.h, 1 if on else 0), "qbg_set_aetrs")
 
     def set_selfconsistent(self, on=True):
         _check(lib().qbg_set_selfconsistent(self.h, 1 if on else 0), "qbg_set_selfconsistent")

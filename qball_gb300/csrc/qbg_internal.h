@@ -155,6 +155,10 @@ struct qbg_plan {
   double* d_hxc_red = nullptr;   // energy partials [3][kHxcBlocks]
   bool have_ionic = false;
   bool selfconsistent = false;
+  bool aetrs = false;            // approximated ETRS (qbg_set_aetrs)
+  int aetrs_stored = 0;          // potentials stored so far (capped at 3)
+  double* d_vhist = nullptr;     // [3][N] v_r at the top of the last three steps
+  size_t vhist_bytes = 0;
   void* adj = nullptr;           // adjoint work buffers (qbg_adjoint.cu)
   double2* fnl_export = nullptr;  // when set: receives (D/Omega)<beta|psi> [nst][nproj] of
                                   // the next H application (device)

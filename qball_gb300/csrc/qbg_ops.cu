@@ -89,6 +89,23 @@ __global__ void k_current(const double2* __restrict__ c, int ld, int ngw,
   }
 }
 
+// SelfConsistentPotential::extrapolate (SelfConsistentPotential.cc:46-73):
+// v = 3 v2 - 3 v1 + 1 v0 in FP64 with the reference's operation order (no
+// contraction), written as the FP64, FP32 and double-float copies the
+// transforms read
+__global__ void k_vextrap(const double* __restrict__ h, long long n, double* __restrict__ vr,
+                          float* __restrict__ vr32, df32* __restrict__ vrdf) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double t = __dadd_rn(__dsub_rn(__dmul_rn(3.0, h[2 * n + i]), __dmul_rn(3.0, h[n + i])),
+                               __dmul_rn(1.0, h[i]));
+    vr[i] = t;
+    const float hi = (float)t;
+    vr32[i] = hi;
+    vrdf[i] = df32(hi, (float)(t - (double)hi));
+  }
+}
+
 qbg_status upload_occ(qbg_plan* p, const double* occ, int nst, double scale,
                              double** d_out, cudaStream_t st) {
   // the reduction buffer's tail holds per-state factors
@@ -513,6 +530,16 @@ qbg_status qbg_gram(qbg_plan* p, double* psi_, int ld, int nst, void* stream) {
   return QBG_OK;
 }
 
+qbg_status qbg_set_aetrs(qbg_plan* p, int on) {
+  if (!p) {
+    set_error("qbg_set_aetrs: null plan");
+    return QBG_ERR_INVALID;
+  }
+  p->aetrs = on != 0;
+  p->aetrs_stored = 0;
+  return QBG_OK;
+}
+
 qbg_status qbg_etrs_step(qbg_plan* p, double* psi_, int ld, int nst, const double* occ,
                          double dt, const double* A_t, const double* A_tdt, double* rho_mid,
                          double* nel, void* stream) {
@@ -534,6 +561,38 @@ qbg_status qbg_etrs_step(qbg_plan* p, double* psi_, int ld, int nst, const doubl
     // loop top: H(t) from the density of psi(t) (EhrenSampleStepper.cc:322-329)
     QBG_TRY(density_any(p, psi, ld, nst, d_occ, p->d_rho, st));
     QBG_TRY(vhxc_update(p, p->d_rho, st));
+  }
+  if (p->aetrs) {
+    // AETRS preupdate (ExponentialWavefunctionStepper.cc:158-163): keep the
+    // potential of H(t); from the third stored step on, the second half step
+    // runs with the potential extrapolated from the last three
+    // (:201-227), and update() does nothing (:247)
+    const size_t nb = sizeof(double) * (size_t)p->N;
+    QBG_TRY(ensure((void**)&p->d_vhist, &p->vhist_bytes, 3 * nb));
+    QBG_CUDA(cudaMemcpyAsync(p->d_vhist, p->d_vhist + p->N, nb, cudaMemcpyDeviceToDevice, st));
+    QBG_CUDA(cudaMemcpyAsync(p->d_vhist + p->N, p->d_vhist + 2 * p->N, nb,
+                             cudaMemcpyDeviceToDevice, st));
+    QBG_CUDA(cudaMemcpyAsync(p->d_vhist + 2 * p->N, p->d_vr, nb, cudaMemcpyDeviceToDevice, st));
+    if (p->aetrs_stored < 3) p->aetrs_stored++;
+    if (p->aetrs_stored >= 3) {
+      QBG_TRY(exponential(p, psi, ld, nst, d_occ, dt1, st));
+      k_vextrap<<<2 * 152 * 4, 256, 0, st>>>(p->d_vhist, p->N, p->d_vr, p->d_vr32, p->d_vrdf);
+      QBG_LAUNCHED(p);
+      QBG_TRY(exponential(p, psi, ld, nst, d_occ, dt1, st));
+      if (rho_mid || nel) {
+        // no predicted state exists in this step: the density returned is
+        // that of psi(t+dt)
+        QBG_TRY(density_any(p, psi, ld, nst, d_occ, rho, st));
+        if (nel) {
+          double s;
+          QBG_TRY(sum_device(p, rho, p->N, &s, st));
+          *nel = s * (p->omega / (double)p->N);
+        }
+      }
+      if (A_tdt) QBG_TRY(qbg_set_vector_potential(p, A_tdt));
+      if (uses_tc(p) && p->check_every_step) QBG_TRY(tc_check_status(p, st));
+      return QBG_OK;
+    }
   }
   // preupdate: psi(t) -> psi(t+dt/2) (kept), -> predicted psi(t+dt) in X
   QBG_TRY(exponential(p, psi, ld, nst, d_occ, dt1, st));

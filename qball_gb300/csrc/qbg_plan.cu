@@ -510,7 +510,8 @@ qbg_status qbg_plan_destroy(qbg_plan* p) {
   void* bufs[] = {p->d_rods, p->d_row_ptr, p->d_row_rod, p->d_row_x, p->d_band_y,
                   p->d_kpgx, p->d_kpg2A, p->d_kpg2A32, p->d_vr, p->d_vr32, p->d_vrdf,
                   p->d_plist, p->d_ptau, p->d_pwt, p->d_pl, p->d_prc, p->d_pdesc, p->d_adesc,
-                  p->d_anl, p->d_anl32, p->d_twnl, p->d_Z, p->d_Y, p->d_fnl, p->d_fpart,
+                  p->d_anl, p->d_anl32, p->d_twnl, p->d_vhist, p->d_Z, p->d_Y, p->d_fnl,
+                  p->d_fpart,
                   p->d_red, p->d_rho, p->d_rho_slots, p->d_vsph, p->d_w[0], p->d_w[1], p->d_w[2], p->d_w[3]};
   for (void* b : bufs)
     if (b) cudaFree(b);

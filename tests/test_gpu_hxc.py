@@ -143,3 +143,30 @@ def test_hxc_state_errors(cuda):
     H.set_density_basis(Q.Basis(cell.L, synth.density_ecut(cell)))
     with pytest.raises(Q.QbgError, match="ionic"):
         H.update_vhxc(rho)
+
+
+@pytest.mark.parametrize("selfconsistent", [True, False])
+def test_aetrs_vs_oracle(cuda, selfconsistent):
+    """AETRS (the stepper's approximated_ option): the first two steps are
+    ETRS steps, from the third on the second half step runs with the
+    extrapolated potential 3 v(t) - 3 v(t-dt) + v(t-2dt); four steps against
+    the oracle's restatement, self-consistent and with a fixed potential."""
+    cell, b, vb, H, oft, hxc, oh, psi, occ, rho0 = hxc_setup("t12", grid=(40, 40, 40))
+    H.update_vhxc(dev(rho0))
+    if selfconsistent:
+        H.set_selfconsistent(True)
+    H.set_aetrs(True)
+    A = synth.kick()
+    p = dev(psi)
+    ref = psi.T.copy()
+    oh.reset_aetrs()
+    l0 = H.launches()
+    for k in range(4):
+        H.etrs_step(p, occ, 0.05, A_t=A, A_tdt=A)
+        ref = oh.aetrs_step(ref, occ, 0.05, A, A, hxc if selfconsistent else None, nthreads=NT)
+        if k == 1:
+            l2 = H.launches()
+    assert rel_err(p.cpu().numpy(), ref.T) < 1e-10
+    assert rel_err(H.get_vlocal(), oh.v_r_now()) < 1e-10
+    # steps 3 and 4 apply H 8 times each instead of 12: fewer launches
+    assert (H.launches() - l2) < (l2 - l0)

@@ -108,3 +108,31 @@ def test_etrs_selfconsistent_conserves_charge_and_couples(cell12):
     ham2 = O.Ham(ft, v0, synth.species(cell))
     p2, _, _ = ham2.etrs_step(psi.T, occ, 0.05, A, A, nthreads=4)
     assert np.abs(p2 - p1).max() > 1e-8
+
+
+def test_oracle_aetrs_fixed_potential_equals_etrs():
+    """With a fixed potential and a constant A, the extrapolated potential is
+    the potential itself and the predictor changes nothing: the oracle's AETRS
+    steps equal its ETRS steps bit for bit."""
+    import qball_gb300 as Q
+    from qball_gb300 import synth
+    from oracle import oracle as O
+    cell = synth.make_cell("t12b")
+    b = O.Basis(Q.cubic_cell(cell.L), cell.ecut)
+    ft = O.FT(b, *cell.grid)
+    v = synth.vlocal(cell)
+    rng = np.random.default_rng(2)
+    c = (rng.standard_normal((b.ngw, 3)) + 1j * rng.standard_normal((b.ngw, 3))) \
+        * np.exp(-b.kpg2 / 8)[:, None]
+    c = O.gram(c)
+    occ = np.full(3, 2.0)
+    A = synth.kick()
+    h1 = O.Ham(ft, v, synth.species(cell))
+    h2 = O.Ham(ft, v, synth.species(cell))
+    h1.set_A(A)
+    h2.set_A(A)
+    x1, x2 = c.copy(), c.copy()
+    for _ in range(4):
+        x1, _, _ = h1.etrs_step(x1, occ, 0.05, A, A)
+        x2 = h2.aetrs_step(x2, occ, 0.05, A, A)
+    assert np.array_equal(x1, x2)
