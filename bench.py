@@ -80,6 +80,9 @@ def parse():
     ap.add_argument("--e2e-warmup", type=int, default=1)
     ap.add_argument("--cpu-states", type=int, default=16)
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--aetrs-steps", type=int, default=3,
+                    help="steps of the headline form with the AETRS propagator option "
+                         "(0: not timed)")
     ap.add_argument("--fp64-slices", type=int, default=7, choices=[6, 7],
                     help="7-bit slices per operand of the FP64 form's tensor-core GEMMs")
     ap.add_argument("--fp64-simt-steps", type=int, default=0,
@@ -564,6 +567,11 @@ def run_ours(args, rank, world, local):
     others = {}
     # (label, form, FP64 GEMM, steps, warm-up); 0 steps: one profiled H|psi> only
     runs = [(f, f, None, args.also_steps, args.also_warmup) for f in args.also.split(",") if f]
+    if args.aetrs_steps:
+        # the same form with the stepper's AETRS option (a different
+        # propagator: 8 H|psi> and one density per step once three
+        # potentials are stored; the warm-up stores them)
+        runs.append((args.form + "_aetrs", args.form, None, args.aetrs_steps, 3))
     if not args.skip_fp64:
         runs.append(("fp64", "fp64", "ozaki", args.fp64_steps, args.fp64_warmup))
         runs.append(("fp64_simt", "fp64", "simt", args.fp64_simt_steps, args.fp64_warmup
@@ -575,6 +583,8 @@ def run_ours(args, rank, world, local):
         H2.set_vector_potential(A)
         if hxc:
             synth.enable_selfconsistent(H2, cell, psi, occ)
+        if label.endswith("_aetrs"):
+            H2.set_aetrs(True)
         p2 = psi.clone()
         ent = {"unit": UNIT, "steps": steps, "warmup": warm,
                "dipole_rel_err_200_steps": acc.get(label)}
