@@ -69,22 +69,25 @@ constexpr int OZ_SMEM = OZ_STAGES * OZ_SLOT + 1024 + 256;
 // (d = 4..7) and 36864 (d = 8); 512 (448 for d = 8) K elements keep every
 // partial sum of the FP32 accumulator below 2^24, hence exact.
 template <int G> struct OzG;
+// ks: 16-K steps per pipeline stage (the stage holds ks x nsl blocks of A
+// and of B; group 0's six MMAs per step are too little work to cover the copy
+// latency with one step per stage)
 template <> struct OzG<0> {  // diagonals 2, 3, 4: slices 1-3
-  static constexpr int nsl = 3, np = 6, nd = 3, win = 32;
+  static constexpr int nsl = 3, np = 6, nd = 3, win = 32, ks = 2;
   __host__ __device__ static constexpr int diag(int k) { return 2 + k; }
   __host__ __device__ static constexpr int ia(int q) { return q == 0 ? 0 : q == 1 ? 0 : q == 2 ? 1 : q == 3 ? 0 : q == 4 ? 1 : 2; }
   __host__ __device__ static constexpr int acc(int q) { return q == 0 ? 0 : q < 3 ? 1 : 2; }
   __host__ __device__ static constexpr int first(int k) { return k == 0 ? 0 : k == 1 ? 1 : 3; }
 };
 template <> struct OzG<1> {  // diagonals 5, 6, 7: slices 1-6
-  static constexpr int nsl = 6, np = 15, nd = 3, win = 32;
+  static constexpr int nsl = 6, np = 15, nd = 3, win = 32, ks = 1;
   __host__ __device__ static constexpr int diag(int k) { return 5 + k; }
   __host__ __device__ static constexpr int acc(int q) { return q < 4 ? 0 : q < 9 ? 1 : 2; }
   __host__ __device__ static constexpr int first(int k) { return k == 0 ? 0 : k == 1 ? 4 : 9; }
   __host__ __device__ static constexpr int ia(int q) { return q - first(acc(q)); }
 };
 template <> struct OzG<2> {  // diagonal 8: slices 1-7
-  static constexpr int nsl = 7, np = 7, nd = 1, win = 28;
+  static constexpr int nsl = 7, np = 7, nd = 1, win = 28, ks = 1;
   __host__ __device__ static constexpr int diag(int) { return 8; }
   __host__ __device__ static constexpr int acc(int) { return 0; }
   __host__ __device__ static constexpr int first(int) { return 0; }
@@ -299,19 +302,25 @@ __device__ __forceinline__ bool oz_produce(const OzArgs& a, const OzCta& c, int 
   using g = OzG<G>;
   const size_t sliceA = (size_t)a.nRTa * a.nK16 * (OZ_BLK / 2);
   const size_t sliceB = (size_t)a.nRTb * a.nK16 * (OZ_BLK / 2);
-  for (int i = 0; i < nks; ++i, ++q) {
+  static_assert(2 * g::ks * g::nsl <= 2 * OZ_SMAX, "stage exceeds its slot");
+  static_assert(g::win % g::ks == 0, "windows hold whole stages");
+  for (int i = 0; i < nks; i += g::ks, ++q) {
     const int s = q % OZ_STAGES;
     if (q >= OZ_STAGES && !mbar_wait(&c.empty[s], ((q / OZ_STAGES) & 1) ^ 1, a.status, a.polls))
       return false;
     if (*c.abort_flag) return false;
+    const int nk = min(g::ks, nks - i);
     unsigned char* st = c.smem + s * OZ_SLOT;
-    mbar_expect_tx(&c.full[s], 2 * g::nsl * OZ_BLK);
-    const size_t oa = ((size_t)mt * a.nK16 + ks0 + i) * (OZ_BLK / 2);
-    const size_t ob = ((size_t)nt * a.nK16 + ks0 + i) * (OZ_BLK / 2);
+    mbar_expect_tx(&c.full[s], 2 * nk * g::nsl * OZ_BLK);
+    for (int kk = 0; kk < nk; ++kk) {
+      const size_t oa = ((size_t)mt * a.nK16 + ks0 + i + kk) * (OZ_BLK / 2);
+      const size_t ob = ((size_t)nt * a.nK16 + ks0 + i + kk) * (OZ_BLK / 2);
 #pragma unroll
-    for (int sl = 0; sl < g::nsl; ++sl) {
-      bulk_g2s(st + sl * OZ_BLK, a.A + sl * sliceA + oa, OZ_BLK, &c.full[s]);
-      bulk_g2s(st + (OZ_SMAX + sl) * OZ_BLK, a.B + sl * sliceB + ob, OZ_BLK, &c.full[s]);
+      for (int sl = 0; sl < g::nsl; ++sl) {
+        bulk_g2s(st + (kk * g::nsl + sl) * OZ_BLK, a.A + sl * sliceA + oa, OZ_BLK, &c.full[s]);
+        bulk_g2s(st + ((g::ks + kk) * g::nsl + sl) * OZ_BLK, a.B + sl * sliceB + ob, OZ_BLK,
+                 &c.full[s]);
+      }
     }
     issued = q + 1;
   }
@@ -340,19 +349,26 @@ __device__ __forceinline__ bool oz_mma(const OzArgs& a, const OzCta& c, uint32_t
       }
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    for (int i = w0; i < w1; ++i, ++q) {
+    for (int i = w0; i < w1; i += g::ks, ++q) {
       const int s = q % OZ_STAGES;
       if (!mbar_wait(&c.full[s], (q / OZ_STAGES) & 1, a.status, a.polls)) return false;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint64_t d0 = sdesc(su32(c.smem + s * OZ_SLOT));
-      const uint32_t first_step = i == w0 ? 1u : 0u;
+      const int nk = min(g::ks, w1 - i);
 #pragma unroll
-      for (int pp = 0; pp < g::np; ++pp) {
-        const int k = g::acc(pp);
-        const uint64_t da = d0 + (uint64_t)((g::ia(pp) * OZ_BLK) >> 4);
-        const uint64_t db = d0 + (uint64_t)(((OZ_SMAX + oz_jb<g>(pp)) * OZ_BLK) >> 4);
-        const uint32_t accf = (pp == g::first(k)) ? (first_step ^ 1u) : 1u;
-        mma_f16(tb[k], da, db, idesc, accf);
+      for (int kk = 0; kk < g::ks; ++kk) {
+        if (kk < nk) {
+          const uint32_t first_step = (i == w0 && kk == 0) ? 1u : 0u;
+#pragma unroll
+          for (int pp = 0; pp < g::np; ++pp) {
+            const int k = g::acc(pp);
+            const uint64_t da = d0 + (uint64_t)(((kk * g::nsl + g::ia(pp)) * OZ_BLK) >> 4);
+            const uint64_t db =
+                d0 + (uint64_t)((((g::ks + kk) * g::nsl + oz_jb<g>(pp)) * OZ_BLK) >> 4);
+            const uint32_t accf = (pp == g::first(k)) ? (first_step ^ 1u) : 1u;
+            mma_f16(tb[k], da, db, idesc, accf);
+          }
+        }
       }
       mma_commit(&c.empty[s]);  // frees the stage once these MMAs are done
     }
