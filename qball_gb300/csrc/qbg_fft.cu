@@ -74,27 +74,46 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
   for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  for (int rl = warp; rl < nl; rl += nw) {
-    const RodInfo ri = rods[r0 + rl];
-    // up to four coefficients per lane loaded before any is stored
-    for (int ib = 0; ib < ri.size; ib += 128) {
-      double2 v[4];
+  // a warp takes up to four rods at once and every lane issues all its loads
+  // (up to 4 x 4 coefficients) before it stores any: the gather is latency
+  // bound, so the more loads in flight the better
+  for (int rb = warp; rb < nl; rb += 4 * nw) {
+    RodInfo ri[4];
+    double2 v[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int rl = rb + r * nw;
+      ri[r] = rl < nl ? rods[r0 + rl] : RodInfo{0, 0, 0, 0};
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int i = ib + lane + 32 * u;
-        if (i < ri.size) v[u] = ps[ri.first + i];
+        const int i = lane + 32 * u;
+        if (i < ri[r].size) v[r][u] = ps[ri[r].first + i];
       }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int rl = rb + r * nw;
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int i = ib + lane + 32 * u;
-        if (i < ri.size) {
-          int z = ri.lmin + i;
+        const int i = lane + 32 * u;
+        if (i < ri[r].size) {
+          int z = ri[r].lmin + i;
           if (z < 0) z += n2;
           C c;
-          c.x = from_f64<T>(v[u].x);
-          c.y = from_f64<T>(v[u].y);
+          c.x = from_f64<T>(v[r][u].x);
+          c.y = from_f64<T>(v[r][u].y);
           A[rl * ls + z] = c;
         }
+      }
+      // rods longer than 128 coefficients
+      for (int i = 128 + lane; i < ri[r].size; i += 32) {
+        const double2 w = ps[ri[r].first + i];
+        int z = ri[r].lmin + i;
+        if (z < 0) z += n2;
+        C c;
+        c.x = from_f64<T>(w.x);
+        c.y = from_f64<T>(w.y);
+        A[rl * ls + z] = c;
       }
     }
   }
@@ -130,9 +149,30 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
   const int nl = min(kTile, nrods - r0);
   const int s = blockIdx.y;
   const C* Zs = Z + (size_t)s * n2 * nrods;
-  for (int it = threadIdx.x; it < nl * n2; it += blockDim.x) {
-    const int rl = it % nl, z = it / nl;
-    A[rl * ls + z] = Zs[(size_t)z * nrods + r0 + rl];
+  {
+    // eight loads in flight per thread before the stores (the Z rows come
+    // from HBM and the load phase is latency bound)
+    constexpr int U = 8;
+    const int tot = nl * n2;
+    for (int it0 = threadIdx.x; it0 < tot; it0 += U * blockDim.x) {
+      C v[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int it = it0 + u * blockDim.x;
+        if (it < tot) {
+          const int rl = it % nl, z = it / nl;
+          v[u] = Zs[(size_t)z * nrods + r0 + rl];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int it = it0 + u * blockDim.x;
+        if (it < tot) {
+          const int rl = it % nl, z = it / nl;
+          A[rl * ls + z] = v[u];
+        }
+      }
+    }
   }
   __syncthreads();
   const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
