@@ -390,8 +390,9 @@ qbg_status qbg_etrs_graph_destroy(qbg_graph* graph);
 /* Autotuner: time H|psi> (two applications after a warm-up) over the
  * plan's transform shapes -- radix order of the Stockham passes (0: 8/4/2
  * first, 1: odd primes first, 2: radix 4 preferred), prime-factor in-place
- * splits on/off, the fused x-y-x kernel on/off, the register lane-group y
- * pass on/off (FP32 transforms) -- then over states per transform launch
+ * splits on/off, the fused x-y-x kernel (whole-plane, band-row, off), the
+ * register lane-group y pass on/off (FP32 transforms) -- then over states
+ * per transform launch
  * group in {8, 16, 32, 64}, and keep the fastest for this plan; *chosen (may
  * be NULL) receives the states per group.  Synchronises. */
 qbg_status qbg_plan_autotune(qbg_plan* plan, const double* psi, int ld, int nst,
@@ -399,13 +400,15 @@ qbg_status qbg_plan_autotune(qbg_plan* plan, const double* psi, int ld, int nst,
 
 /* Transform shape of a plan (what qbg_plan_autotune searches; every shape
  * gives the same results to rounding): radix_order 0..2 as above,
- * prime_factor / fused / lane_group 0 or 1.  Synchronises when the radix
- * order changes (the tables are rebuilt). */
+ * prime_factor / lane_group 0 or 1, fused 0 (separate x, y, x kernels),
+ * 1 (band-row fused kernel) or 2 (whole-plane kernel on 120 x 120 planes,
+ * the default; other planes run as 1).  Synchronises when the radix order
+ * changes (the tables are rebuilt). */
 qbg_status qbg_plan_set_transform_config(qbg_plan* plan, int radix_order,
                                          int prime_factor, int fused,
                                          int lane_group);
 /* cfg (host int[5]): states per group, radix order, prime-factor splits,
- * fused x-y-x kernel, lane-group y pass. */
+ * fused x-y-x kernel (0..2), lane-group y pass. */
 qbg_status qbg_plan_get_transform_config(const qbg_plan* plan, int* cfg);
 
 /* Diagnostic, no reference counterpart: runs one bounded mbarrier wait that

@@ -93,7 +93,7 @@ ABI = {
     "qbg_profile_read": [_P, _P, _P, _I],
     "qbg_phase_name": [_I],
 }
-NPHASE = 13
+NPHASE = 14
 
 
 class QbgError(RuntimeError):
@@ -247,7 +247,9 @@ class FourierTransform:
         _check(lib().qbg_plan_set_fp64_gemm(self.h, m, int(slices)), "qbg_plan_set_fp64_gemm")
         self.fp64_gemm, self.oz_slices = mode, int(slices)
 
-    def set_transform_config(self, radix_order=0, prime_factor=1, fused=1, lane_group=1):
+    def set_transform_config(self, radix_order=0, prime_factor=1, fused=2, lane_group=1):
+        """fused: 2 whole-plane kernel on 120 x 120 planes (band-row kernel
+        elsewhere), 1 band-row fused kernel, 0 separate x, y, x kernels."""
         _check(lib().qbg_plan_set_transform_config(self.h, int(radix_order), int(prime_factor),
                                                    int(fused), int(lane_group)),
                "qbg_plan_set_transform_config")

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libqbg.so")
 BUILD = os.path.join(HERE, "_build")
-SOURCES = ["qbg_plan.cu", "qbg_fft.cu", "qbg_nl.cu", "qbg_ops.cu", "qbg_tc.cu", "qbg_ozaki.cu",
+SOURCES = ["qbg_plan.cu", "qbg_fft.cu", "qbg_plane.cu", "qbg_nl.cu", "qbg_ops.cu", "qbg_tc.cu", "qbg_ozaki.cu",
            "qbg_noalloc.cu", "qbg_hxc.cu", "qbg_graph.cu", "qbg_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",

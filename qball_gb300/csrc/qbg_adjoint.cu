@@ -74,7 +74,8 @@ struct AdjWork {
   double2* chi = nullptr;        // P_b^+ lambda
   double2* lf[4] = {};           // (D/Omega) <beta|H^j y0>, j = 0..3
   size_t lf_bytes = 0;
-  double2* fields = nullptr; size_t fields_bytes = 0;  // [8][chunk][N] real space
+  double2* fields = nullptr; size_t fields_bytes = 0;  // [8][chunk][N] real space (or the
+                                                       // whole-plane field and slots)
   double2* proj = nullptr; size_t proj_bytes = 0;      // [12][nst][P]
   double* part = nullptr; size_t part_bytes = 0;       // block partial sums
   double* occ = nullptr; size_t occ_bytes = 0;         // per-state occupations
@@ -372,7 +373,18 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* const* x,
     QBG_TRY(comb(p, yv, cm, 4 - m, ld, p->ngw, nst, w->Y[3 - m], st));
   }
   const double2* M[4] = {w->Y[3], w->Y[2], w->Y[1], w->Y[0]};
-  if (grad_v) {
+  const bool tr32 = p->prec != QBG_PREC_FP64 && p->prec != QBG_PREC_MIXED_FFT64 &&
+                    p->prec != QBG_PREC_MIXED_DF32;
+  if (grad_v && plane_applies(p, tr32)) {
+    // whole planes: bwd(M_m) kept as one field in the transform type, the
+    // transform of x_m multiplied into per-state slots in its last pass
+    const int ch = std::max(1, std::min(p->chunk, nst));
+    QBG_TRY(ensure((void**)&w->fields, &w->fields_bytes, plane_pair_bytes(p, ch)));
+    if (p->prec == QBG_PREC_MIXED_DF32)
+      QBG_TRY(pair_grad<df32>(p, M, x, 4, ld, nst, 2.0 / (double)p->N, grad_v, w->fields, st));
+    else
+      QBG_TRY(pair_grad<double>(p, M, x, 4, ld, nst, 2.0 / (double)p->N, grad_v, w->fields, st));
+  } else if (grad_v) {
     const int ch = std::max(1, std::min(p->chunk, nst));
     QBG_TRY(ensure((void**)&w->fields, &w->fields_bytes, sizeof(double2) * 8 * (size_t)ch * p->N));
     for (int s0 = 0; s0 < nst; s0 += ch) {

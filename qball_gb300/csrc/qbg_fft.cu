@@ -58,7 +58,7 @@ template <typename T> __device__ __forceinline__ cplx<T> czero() {
 // ------------------------------------------------------------------ z pass
 // backward: gather rods of state blockIdx.y from the sphere, transform
 // along z, write Z[s][z][rod].
-template <typename T, bool BIGP>
+template <typename T, bool BIGP, bool L120 = false>
 __global__ void __launch_bounds__(kThreads)
 k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
         const RodInfo* __restrict__ rods, int nrods, FFTLen<T> d) {
@@ -118,7 +118,9 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
     }
   }
   __syncthreads();
-  const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
+  const C* R = A;
+  if constexpr (L120) pfa120_inplace_lines<+1>(A, ls, nl);
+  else R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
   C* Zs = Z + (size_t)blockIdx.y * n2 * nrods;
   for (int it = threadIdx.x; it < nl * n2; it += blockDim.x) {
     const int rl = it % nl, z = it / nl;
@@ -130,7 +132,7 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
 // the sphere with the epilogue of MODE:
 //   0 store       c[g] = val
 //   1 hpsi        o = (o_nl + kin*psi) + val; out[g] = o; acc[g] += fac*o
-template <typename T, int MODE, bool BIGP>
+template <typename T, int MODE, bool BIGP, bool L120 = false>
 __global__ void __launch_bounds__(kThreads)
 k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
         const RodInfo* __restrict__ rods, int nrods, FFTLen<T> d, T scale,
@@ -175,7 +177,9 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
     }
   }
   __syncthreads();
-  const C* R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
+  const C* R = A;
+  if constexpr (L120) pfa120_inplace_lines<-1>(A, ls, nl);
+  else R = fft_lines<-1, T, BIGP>(A, B, nl, ls, dv);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double2* os = out + (size_t)s * ldo;
   if constexpr (MODE == 2) {
@@ -923,16 +927,28 @@ static bool big_prime(const LenTables& L) {
 
 // The launchers below work on the plan's Z and Y intermediates unless the
 // caller passes its own (Z, Y: the same shapes for ns states).
+// z lines of 120 points as the in-place three-pass prime-factor transform
+// (with the whole-plane kernels: the plan's fused mode 2)
+template <typename T> static bool z_inplace120(const qbg_plan* p, const FFTLen<T>& d) {
+  return d.n == 120 && d.pfa && p->fuse_xyx && p->plane_xyx;
+}
+
 template <typename T, bool BIGP>
 static qbg_status run_z_bwd_(qbg_plan* p, const double2* c, int ldc, int ns, cudaStream_t st,
                              void* Z) {
   const FFTLen<T> d = p->len[2].view<T>();
   const size_t sm = smem_bytes<T>(d, false, nthreads_z(d));
-  QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   PhaseTimer pt(p, PH_Z_BWD, st);
-  k_z_bwd<T, BIGP><<<grid, nthreads_z(d), sm, st>>>(c, ldc, (cplx<T>*)(Z ? Z : p->d_Z), p->d_rods,
-                                                    p->nrods, d);
+  if (!BIGP && z_inplace120(p, d)) {
+    QBG_CUDA(prep(k_z_bwd<T, false, true>, sm));
+    k_z_bwd<T, false, true><<<grid, nthreads_z(d), sm, st>>>(
+        c, ldc, (cplx<T>*)(Z ? Z : p->d_Z), p->d_rods, p->nrods, d);
+  } else {
+    QBG_CUDA(prep(k_z_bwd<T, BIGP>, sm));
+    k_z_bwd<T, BIGP><<<grid, nthreads_z(d), sm, st>>>(c, ldc, (cplx<T>*)(Z ? Z : p->d_Z),
+                                                      p->d_rods, p->nrods, d);
+  }
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
@@ -1062,14 +1078,21 @@ static qbg_status run_z_fwd_(qbg_plan* p, double2* out, int ldo, int ns, const d
                              cudaStream_t st) {
   const FFTLen<T> d = p->len[2].view<T>();
   const size_t sm = smem_bytes<T>(d, false, nthreads_z(d));
-  QBG_CUDA(prep(k_z_fwd<T, MODE, BIGP>, sm));
   dim3 grid((p->nrods + kTile - 1) / kTile, ns);
   const T scale = (T)(1.0 / (double)(p->np0 * p->np1 * p->np2));
   const double* kin = p->d_kpg2A;
   PhaseTimer pt(p, PH_Z_FWD, st);
-  k_z_fwd<T, MODE, BIGP><<<grid, nthreads_z(d), sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
-                                                    p->d_rods, p->nrods, d, scale, psi, ldp,
-                                                    kin, out_init, acc, lda, fac);
+  if (!BIGP && z_inplace120(p, d)) {
+    QBG_CUDA(prep(k_z_fwd<T, MODE, false, true>, sm));
+    k_z_fwd<T, MODE, false, true><<<grid, nthreads_z(d), sm, st>>>(
+        (const cplx<T>*)p->d_Z, out, ldo, p->d_rods, p->nrods, d, scale, psi, ldp, kin,
+        out_init, acc, lda, fac);
+  } else {
+    QBG_CUDA(prep(k_z_fwd<T, MODE, BIGP>, sm));
+    k_z_fwd<T, MODE, BIGP><<<grid, nthreads_z(d), sm, st>>>((const cplx<T>*)p->d_Z, out, ldo,
+                                                      p->d_rods, p->nrods, d, scale, psi, ldp,
+                                                      kin, out_init, acc, lda, fac);
+  }
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
@@ -1177,11 +1200,14 @@ qbg_status local_hpsi(qbg_plan* p, const double2* psi, int ld, double2* out, int
   const int ch = std::max(1, std::min(p->chunk, nst));
   QBG_TRY(ensure_scratch<T>(p, ch));
   size_t xyx_smem = 0;
-  const int G = xyx_group<T>(p, &xyx_smem);
+  const bool plane = plane_applies(p, std::is_same<T, float>::value);
+  const int G = plane ? 0 : xyx_group<T>(p, &xyx_smem);
   for (int s0 = 0; s0 < nst; s0 += ch) {
     const int ns = std::min(ch, nst - s0);
     QBG_TRY(run_z_bwd<T>(p, psi + (size_t)s0 * ld, ld, ns, st));
-    if (G) {
+    if (plane) {
+      if constexpr (!std::is_same<T, float>::value) QBG_TRY(plane_vloc<T>(p, ns, st));
+    } else if (G) {
       if constexpr (!std::is_same<T, float>::value) QBG_TRY(run_xyx<T>(p, ns, G, xyx_smem, st));
     } else {
       QBG_TRY(run_x<T>(p, true, ns, st));
@@ -1214,11 +1240,43 @@ qbg_status backward(qbg_plan* p, const double2* c, int ldc, double2* f, int nb, 
   for (int s0 = 0; s0 < nb; s0 += ch) {
     const int ns = std::min(ch, nb - s0);
     QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ldc, ldc, ns, st));
+    if (plane_applies(p, std::is_same<T, float>::value)) {
+      if constexpr (!std::is_same<T, float>::value)
+        QBG_TRY(plane_field<T>(p, ns, f + (size_t)s0 * p->N, st));
+      continue;
+    }
     QBG_TRY(run_x<T>(p, true, ns, st));
     QBG_TRY((run_y<T, Y_BWD_STORE>(p, ns, f + (size_t)s0 * p->N, nullptr, nullptr, 0, st)));
   }
   return QBG_OK;
 }
+
+template <typename T>
+qbg_status pair_grad(qbg_plan* p, const double2* const* M, const double2* const* X, int nm,
+                     int ld, int nst, double scale, double* grad, void* work, cudaStream_t st) {
+  if constexpr (std::is_same<T, float>::value) {
+    set_error("pair_grad: no whole-plane kernel for FP32 transforms");
+    return QBG_ERR_UNSUPPORTED;
+  } else {
+    const int ch = std::max(1, std::min(p->chunk, nst));
+    QBG_TRY(ensure_scratch<T>(p, ch));
+    for (int s0 = 0; s0 < nst; s0 += ch) {
+      const int ns = std::min(ch, nst - s0);
+      for (int m = 0; m < nm; ++m) {
+        QBG_TRY(run_z_bwd<T>(p, M[m] + (size_t)s0 * ld, ld, ns, st));
+        QBG_TRY(plane_pair_field<T>(p, ns, work, st));
+        QBG_TRY(run_z_bwd<T>(p, X[m] + (size_t)s0 * ld, ld, ns, st));
+        QBG_TRY(plane_pair<T>(p, ns, work, m > 0 ? 1 : 0, st));
+      }
+      QBG_TRY(plane_pair_sum<T>(p, ns, work, scale, grad, st));
+    }
+    return QBG_OK;
+  }
+}
+template qbg_status pair_grad<double>(qbg_plan*, const double2* const*, const double2* const*,
+                                      int, int, int, double, double*, void*, cudaStream_t);
+template qbg_status pair_grad<df32>(qbg_plan*, const double2* const*, const double2* const*,
+                                    int, int, int, double, double*, void*, cudaStream_t);
 
 template <typename T>
 qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb, cudaStream_t st) {
@@ -1227,8 +1285,13 @@ qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb, cudaStr
   const double2 zero = make_double2(0.0, 0.0);
   for (int s0 = 0; s0 < nb; s0 += ch) {
     const int ns = std::min(ch, nb - s0);
-    QBG_TRY((run_y<T, Y_FWD_LOAD>(p, ns, f + (size_t)s0 * p->N, nullptr, nullptr, 0, st)));
-    QBG_TRY(run_x<T>(p, false, ns, st));
+    if (plane_applies(p, std::is_same<T, float>::value)) {
+      if constexpr (!std::is_same<T, float>::value)
+        QBG_TRY(plane_fwd<T>(p, ns, f + (size_t)s0 * p->N, st));
+    } else {
+      QBG_TRY((run_y<T, Y_FWD_LOAD>(p, ns, f + (size_t)s0 * p->N, nullptr, nullptr, 0, st)));
+      QBG_TRY(run_x<T>(p, false, ns, st));
+    }
     QBG_TRY((run_z_fwd<T, 0>(p, c + (size_t)s0 * ldc, ldc, ns, nullptr, 0, 0, nullptr, 0, zero,
                              st)));
   }
@@ -1248,11 +1311,15 @@ qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst, const double
   QBG_TRY(ensure((void**)&p->d_rho_slots, &p->rho_slots_bytes,
                  sizeof(double) * (size_t)p->N * ch));
   size_t xy_smem = 0;
-  const int G = xy_density_group<T>(p, &xy_smem);
+  const bool plane = plane_applies(p, std::is_same<T, float>::value);
+  const int G = plane ? 0 : xy_density_group<T>(p, &xy_smem);
   for (int s0 = 0; s0 < nst; s0 += ch) {
     const int ns = std::min(ch, nst - s0);
     QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ldc, ldc, ns, st));
-    if (G) {
+    if (plane) {
+      if constexpr (!std::is_same<T, float>::value)
+        QBG_TRY(plane_density<T>(p, ns, d_w + s0, s0 > 0 ? 1 : 0, p->d_rho_slots, st));
+    } else if (G) {
       if constexpr (!std::is_same<T, float>::value)
         QBG_TRY(run_xy_density<T>(p, ns, d_w + s0, s0 > 0 ? 1 : 0, G, xy_smem, st));
     } else {
@@ -1263,7 +1330,7 @@ qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst, const double
   }
   {
     PhaseTimer pt(p, PH_Y_DENSITY, st);
-    if (G && std::is_same<T, df32>::value)
+    if ((G || plane) && std::is_same<T, df32>::value)
       k_sum_slots<df32><<<2 * 152 * 4, 256, 0, st>>>((const df32*)p->d_rho_slots, ch, p->N, rho);
     else
       k_sum_slots<double><<<2 * 152 * 4, 256, 0, st>>>(p->d_rho_slots, ch, p->N, rho);

@@ -208,9 +208,11 @@ qbg_status qbg_plan_autotune(qbg_plan* p, const double* psi, int ld, int nst, co
   const bool fp32 = p->prec == QBG_PREC_MIXED || p->prec == QBG_PREC_MIXED_NL64;
   for (int order = 0; order < 3 && s == QBG_OK; ++order)
     for (int pfa = 1; pfa >= 0 && s == QBG_OK; --pfa)
-      for (int fused = 1; fused >= 0 && s == QBG_OK; --fused)
+      for (int fused = 2; fused >= 0 && s == QBG_OK; --fused)
         for (int lane = 1; lane >= (fp32 ? 0 : 1) && s == QBG_OK; --lane) {
           if (!pfa && fused) continue;  // the fused kernels need the prime-factor splits
+          // the whole-plane kernel: 120 x 120 planes, FP64 or double-float
+          if (fused == 2 && (fp32 || p->np0 != 120 || p->np1 != 120)) continue;
           s = qbg_plan_set_transform_config(p, order, pfa, fused, lane);
           float ms = 0.f;
           if (s == QBG_OK) s = time_h(&ms);

@@ -52,7 +52,8 @@ struct LenTables {
 // "fnl_gemm", "enl_hpsi" in NonLocalPotential.cc:2059-2170).
 enum Phase {
   PH_FNL_GEMM = 0, PH_FNL_REDUCE, PH_ENL_HPSI, PH_Z_BWD, PH_X_BWD, PH_Y_VLOC,
-  PH_X_FWD, PH_Z_FWD, PH_Y_DENSITY, PH_Y_STORE, PH_Y_LOAD, PH_MISC, PH_XYX_VLOC, PH_COUNT
+  PH_X_FWD, PH_Z_FWD, PH_Y_DENSITY, PH_Y_STORE, PH_Y_LOAD, PH_MISC, PH_XYX_VLOC, PH_XY_PAIR,
+  PH_COUNT
 };
 extern const char* const kPhaseName[PH_COUNT];
 
@@ -125,6 +126,7 @@ struct qbg_plan {
   int tc_polls = -1;            // poll limit of the GEMM pipeline waits (-1: default)
   bool lane_fft = true;         // register-resident lane-group transforms where supported
   bool fuse_xyx = true;         // x, y and x passes of H psi in one kernel where they fit
+  bool plane_xyx = true;        // ... as the whole-plane kernel on 120 x 120 planes
   int radix_order = 0;          // Stockham radix order of the length tables (factorize)
 
   // scratch (allocated lazily, grown as needed)
@@ -217,6 +219,31 @@ qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb,
 template <typename T>
 qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst,
                    const double* d_w, double* rho, cudaStream_t st);
+// dL/dv(r) of the adjoint on whole planes (120 x 120, FP64 or double-float
+// transforms): grad[r] += scale * sum_s sum_{m < nm} Re(conj(bwd(M_m))
+// bwd(X_m)) over the states, work holding plane_pair_bytes(p, chunk) bytes
+template <typename T>
+qbg_status pair_grad(qbg_plan* p, const double2* const* M, const double2* const* X, int nm,
+                     int ld, int nst, double scale, double* grad, void* work, cudaStream_t st);
+
+// whole-plane kernels (qbg_plane.cu): 120 x 120 planes, FP64 or
+// double-float transforms, the plan's fused mode 2
+bool plane_applies(const qbg_plan* p, bool fp32);
+template <typename T> qbg_status plane_vloc(qbg_plan* p, int ns, cudaStream_t st);
+template <typename T>
+qbg_status plane_density(qbg_plan* p, int ns, const double* w, int acc, void* slots,
+                         cudaStream_t st);
+template <typename T> qbg_status plane_field(qbg_plan* p, int ns, double2* f, cudaStream_t st);
+template <typename T>
+qbg_status plane_fwd(qbg_plan* p, int ns, const double2* f, cudaStream_t st);
+size_t plane_pair_bytes(const qbg_plan* p, int ns);
+template <typename T> qbg_status plane_pair_field(qbg_plan* p, int ns, void* work, cudaStream_t st);
+template <typename T>
+qbg_status plane_pair(qbg_plan* p, int ns, void* work, int acc, cudaStream_t st);
+template <typename T>
+qbg_status plane_pair_sum(qbg_plan* p, int ns, const void* work, double scale, double* grad,
+                          cudaStream_t st);
+
 template <typename T>
 qbg_status backward_scratch(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,
                             void* Z, void* Y, int chunk, cudaStream_t st);

@@ -223,6 +223,91 @@ __device__ __forceinline__ void pfa120_lines(C* L, int ls, int nl) {
   __syncthreads();
 }
 
+// ---- 120 points in place and in order ------------------------------------
+// The same Ruritanian map n = (15 n1 + 40 a + 24 b) mod 120 (n1 < 8, a < 3,
+// b < 5) for input and output (Burrus and Eschenbacher, 1981): n k = 105 n1
+// k1 + 40 a ka + 96 b kb (mod 120), so for the direction s the transform is
+// a 3-point DFT over a with exp(s 2 pi i / 3), a 5-point DFT over b with
+// exp(s 2 pi i 4/5) = exp(-s 2 pi i / 5) and an 8-point DFT over n1 with
+// exp(s 2 pi i 7/8) = exp(-s 2 pi i / 8).  Each item of each pass reads
+// and writes the same slots: items are independent, the passes commute, and
+// nothing is held in registers across a barrier.
+__host__ __device__ __forceinline__ int pl_m120(int x) { return x >= 120 ? x - 120 : x; }
+
+// slots of item j of in-place pass P (0: 3-point over a, 1: 5-point over b, 2:
+// 8-point over n1): i[0] first, consecutive slots STEP apart mod 120
+template <int P> struct PlPass;
+template <> struct PlPass<0> {  // j = 5 n1 + b < 40
+  static constexpr int R = 3, NI = 40, STEP = 40;
+  __device__ __forceinline__ static int base(int j) {
+    const int n1 = j / 5, b = j - 5 * n1;
+    return pl_m120(15 * n1 + 24 * b);
+  }
+};
+template <> struct PlPass<1> {  // j = 3 n1 + a < 24
+  static constexpr int R = 5, NI = 24, STEP = 24;
+  __device__ __forceinline__ static int base(int j) {
+    const int n1 = j / 3, a = j - 3 * n1;
+    return pl_m120(15 * n1 + 40 * a);
+  }
+};
+template <> struct PlPass<2> {  // j = 5 a + b < 15
+  static constexpr int R = 8, NI = 15, STEP = 15;
+  __device__ __forceinline__ static int base(int j) {
+    const int a = j / 5, b = j - 5 * a;
+    return pl_m120(40 * a + 24 * b);
+  }
+};
+
+template <int P> __device__ __forceinline__ void pl_slots(int j, int* i) {
+  i[0] = PlPass<P>::base(j);
+#pragma unroll
+  for (int k = 1; k < PlPass<P>::R; ++k) i[k] = pl_m120(i[k - 1] + PlPass<P>::STEP);
+}
+
+// the pass' codelet for direction S (+1 backward, -1 forward)
+template <int P, int S, typename C> __device__ __forceinline__ void pl_dft(C* v) {
+  if constexpr (P == 0) dft3<S>(v);
+  else if constexpr (P == 1) dft5<-S>(v);
+  else dft8<-S>(v);
+}
+
+// one item of pass P on the line at ln (element stride ST)
+template <int P, int S, int ST, typename C>
+__device__ __forceinline__ void pl_item(C* ln, int j) {
+  constexpr int R = PlPass<P>::R;
+  int i[R];
+  pl_slots<P>(j, i);
+  C v[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) v[k] = ln[i[k] * ST];
+  pl_dft<P, S>(v);
+#pragma unroll
+  for (int k = 0; k < R; ++k) ln[i[k] * ST] = v[k];
+}
+
+// all three in-place passes (direction S) over nl lines of 120 points, line
+// stride ls, lines fastest across threads; ends with a barrier
+template <int S, typename C>
+__device__ __forceinline__ void pfa120_inplace_lines(C* L, int ls, int nl) {
+  const float inl = 1.f / (float)nl;
+  for (int it = threadIdx.x; it < nl * PlPass<0>::NI; it += blockDim.x) {
+    const int j = divf(it, inl), line = it - j * nl;
+    pl_item<0, S, 1>(L + line * ls, j);
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < nl * PlPass<1>::NI; it += blockDim.x) {
+    const int j = divf(it, inl), line = it - j * nl;
+    pl_item<1, S, 1>(L + line * ls, j);
+  }
+  __syncthreads();
+  for (int it = threadIdx.x; it < nl * PlPass<2>::NI; it += blockDim.x) {
+    const int j = divf(it, inl), line = it - j * nl;
+    pl_item<2, S, 1>(L + line * ls, j);
+  }
+  __syncthreads();
+}
+
 // prime-factor split used for length n (0: none; the Stockham engine runs)
 __host__ __device__ inline int pfa_split(int n) {
   switch (n) {

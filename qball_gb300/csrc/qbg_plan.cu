@@ -16,7 +16,8 @@ static thread_local std::string g_err;
 
 const char* const kPhaseName[PH_COUNT] = {
     "fnl_gemm", "fnl_reduce", "enl_hpsi", "ft_z_bwd", "ft_x_bwd", "ft_y_vloc",
-    "ft_x_fwd", "ft_z_fwd", "ft_y_density", "ft_y_store", "ft_y_load", "misc", "ft_xyx_vloc"};
+    "ft_x_fwd", "ft_z_fwd", "ft_y_density", "ft_y_store", "ft_y_load", "misc", "ft_xyx_vloc",
+    "ft_xy_pair"};
 
 void set_error(const char* fmt, ...) {
   char buf[512];
@@ -653,8 +654,8 @@ qbg_status qbg_plan_set_chunk(qbg_plan* p, int states) {
 
 qbg_status qbg_plan_set_transform_config(qbg_plan* p, int radix_order, int prime_factor,
                                          int fused, int lane_group) {
-  if (!p || radix_order < 0 || radix_order > 2) {
-    set_error("qbg_plan_set_transform_config: radix_order must be 0, 1 or 2");
+  if (!p || radix_order < 0 || radix_order > 2 || fused < 0 || fused > 2) {
+    set_error("qbg_plan_set_transform_config: radix_order and fused must be 0, 1 or 2");
     return QBG_ERR_INVALID;
   }
   if (radix_order != p->radix_order) {
@@ -674,6 +675,7 @@ qbg_status qbg_plan_set_transform_config(qbg_plan* p, int radix_order, int prime
   }
   for (auto& L : p->len) L.allow_pfa = prime_factor != 0;
   p->fuse_xyx = fused != 0;
+  p->plane_xyx = fused == 2;
   p->lane_fft = lane_group != 0;
   return QBG_OK;
 }
@@ -686,7 +688,7 @@ qbg_status qbg_plan_get_transform_config(const qbg_plan* p, int* cfg) {
   cfg[0] = p->chunk;
   cfg[1] = p->radix_order;
   cfg[2] = p->len[0].allow_pfa ? 1 : 0;
-  cfg[3] = p->fuse_xyx ? 1 : 0;
+  cfg[3] = p->fuse_xyx ? (p->plane_xyx ? 2 : 1) : 0;
   cfg[4] = p->lane_fft ? 1 : 0;
   return QBG_OK;
 }

@@ -7,6 +7,8 @@
 - dL/dv(r) and dL/d(pulse amplitudes) of a dipole loss over a laser-driven
   run agree with central finite differences of the FP64 forward (1e-6);
 - the gradients do not depend on the checkpoint interval (1e-13);
+- on 120 x 120 planes the whole-plane pair-product gradient equals the
+  eight-field path (FP64 1e-12, mixed_df32 1e-10);
 - the reduced-precision forms' gradients against the FP64 adjoint
   (mixed_df32 1e-8, mixed 1e-5; observed 1.2e-10 and 1.3e-7).
 """
@@ -205,3 +207,24 @@ def test_gradients_match_oracle_adjoint(cuda):
     assert abs(L - Lo) < 1e-10 * abs(Lo)
     assert rel_err(gv, gvo) < 1e-8, rel_err(gv, gvo)
     assert rel_err(gk, gko) < 1e-8, rel_err(gk, gko)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("mixed_df32", 1e-10)])
+def test_whole_plane_gradient_matches_field_path(cuda, prec, tol):
+    """dL/dv(r) on the 216-atom cell's 120^3 grid through the whole-plane
+    pair-product kernel (fused mode 2: bwd(M_m) kept as one field, the
+    transform of x_m multiplied into per-state slots in its last pass)
+    against the path that stores all eight real-space fields per state
+    (fused mode 1); dL/da_k alike.  40 states: a full 32-state chunk and a
+    last chunk of 8."""
+    N = 2
+    ak, G = laser(N)
+    dstar = ad.target_dipole(N, scale=2e-3)
+    cell, H, v, psi, occ = setup("c2", prec, natoms=8, nst=40)
+    res = {}
+    for fused in (1, 2):
+        H.set_transform_config(0, 1, fused, 1)
+        res[fused] = _grads(H, psi, occ, ak, G, N, 1, dstar)
+    assert abs(res[2][0] - res[1][0]) < tol * abs(res[1][0])
+    assert rel_err(res[2][1], res[1][1]) < tol
+    assert rel_err(res[2][2], res[1][2]) < tol

@@ -73,12 +73,14 @@ def test_fft_backward_forward_vs_reference_golden(cuda, name):
                                          (20.0, 10.0, (48, 48, 48)), (10.0, 6.0, (28, 28, 28)),
                                          (10.0, 6.0, (22, 22, 26)),
                                          (12.0, 10.0, (120, 48, 40)),
+                                         (12.0, 10.0, (120, 120, 40)),
                                          (12.0, 10.0, (72, 80, 144)),
                                          (12.0, 10.0, (160, 36, 50))])
 def test_fft_vs_oracle_many_grids(cuda, L, ecut, grid):
     """radix 2,3,4,5,8, the direct-DFT primes 7, 11 and 13, and the
     prime-factor lengths 120 = 8x15, 48 = 16x3, 40 = 8x5, 72 = 8x9,
-    80 = 16x5, 144 = 16x9, and 160 (the 512-atom cell's length, Stockham)"""
+    80 = 16x5, 144 = 16x9, and 160 (the 512-atom cell's length, Stockham);
+    120 x 120 planes run through the whole-plane kernels"""
     b = Q.Basis(L, ecut)
     ob = O.Basis(b.a, ecut)
     oft = O.FT(ob, *grid)
@@ -161,6 +163,45 @@ def test_hpsi_216_atom_grid_full_chunk(cuda, prec, tol):
     ref, enl_ref = oh.hpsi(psi.T, occ, nthreads=NT)
     assert rel_err(out.cpu().numpy(), ref.T) < tol
     assert abs(enl - enl_ref) <= tol * abs(enl_ref)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("mixed_df32", 1e-11)])
+def test_density_216_atom_grid(cuda, prec, tol):
+    """The density on the 216-atom cell's 120^3 grid (the whole-plane kernel:
+    x and y transforms of a plane and w |psi(r)|^2 in one CTA) against the
+    oracle, 40 states: a full 32-state chunk and an accumulating chunk of 8."""
+    cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=40)
+    occ = synth.occupations(cell)
+    torch = _torch()
+    rho = torch.zeros(oft.n012, dtype=torch.float64, device=cuda)
+    nel = H.update_density(dev(psi), occ, rho)
+    rref, nref = O.update_density(oft, psi.T, occ, nthreads=NT)
+    assert rel_err(rho.cpu().numpy(), rref) < tol
+    assert abs(nel - nref) < tol * nref
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("mixed_df32", 1e-12)])
+def test_plane_kernel_matches_band_row_kernels(cuda, prec, tol):
+    """On 120 x 120 planes the whole-plane kernel (fused 2), the band-row
+    fused kernel (1) and the separate x, y, x kernels (0) give the same
+    H|psi> and density to the rounding of the transform arithmetic."""
+    cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=6)
+    occ = synth.occupations(cell)
+    torch = _torch()
+    p = dev(psi)
+    outs, rhos = [], []
+    for fused in (2, 1, 0):
+        H.set_transform_config(0, 1, fused, 1)
+        assert H.transform_config()["fused"] == fused
+        out = torch.zeros_like(p)
+        H.hpsi(p, out, occ)
+        rho = torch.zeros(oft.n012, dtype=torch.float64, device=cuda)
+        H.update_density(p, occ, rho)
+        outs.append(out.cpu().numpy())
+        rhos.append(rho.cpu().numpy())
+    for k in (1, 2):
+        assert rel_err(outs[k], outs[0]) < tol, k
+        assert rel_err(rhos[k], rhos[0]) < tol, k
 
 
 @pytest.mark.parametrize("name", ["c1", "c1q"])
