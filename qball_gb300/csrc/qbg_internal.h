@@ -127,6 +127,7 @@ struct qbg_plan {
   bool lane_fft = true;         // register-resident lane-group transforms where supported
   bool fuse_xyx = true;         // x, y and x passes of H psi in one kernel where they fit
   bool plane_xyx = true;        // ... as the whole-plane kernel on 120 x 120 planes
+  int nsm = 0;                  // SMs of the plan's device (set on first use)
   int radix_order = 0;          // Stockham radix order of the length tables (factorize)
 
   // scratch (allocated lazily, grown as needed)

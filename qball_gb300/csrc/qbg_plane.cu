@@ -142,52 +142,114 @@ __device__ __forceinline__ void pl_backward_to_last(cplx<T>* Pl, const cplx<T>* 
   pl_cols<1, +1>(Pl);
 }
 
-// H psi middle for one (plane z, state s): Z row of rods -> x backward ->
-// y backward -> v(r) product -> y forward -> x forward -> Z row of rods.
-// v holds the plane-major local potential in the transform arithmetic T.
-template <typename T>
+// 16-byte asynchronous copies global -> shared (cp.async: the hardware
+// completes them, no wait loop of ours)
+__device__ __forceinline__ void pl_cp16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(
+                   (unsigned)__cvta_generic_to_shared(dst)),
+               "l"(src));
+}
+__device__ __forceinline__ void pl_cp_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void pl_cp_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// H psi middle for (plane z, state s) work items w = z + n2 s: Z row of rods
+// -> x backward -> y backward -> v(r) product -> y forward -> x forward -> Z
+// row of rods.  v holds the plane-major local potential in the transform
+// arithmetic T.  Persistent CTAs walk the items with a grid stride.  With
+// STAGE (the Z row fits in the plane's non-band rows), the next
+// item's Z row is copied into the non-band rows while the x forward passes
+// of the current one run there on the band rows only, so the next plane
+// fills from shared memory instead of waiting on HBM.
+template <typename T, bool STAGE>
 __global__ void __launch_bounds__(kPlThreads, 1)
 k_plane_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
-             const int* __restrict__ row_xb, int nband, int n2, const T* __restrict__ v) {
+             const int* __restrict__ row_xb, int nband, int n2, int ns,
+             const T* __restrict__ v) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   C* Pl = reinterpret_cast<C*>(smem);
-  const int z = blockIdx.x, s = blockIdx.y;
   const int ntr = nband / 2 + (nband & 1);
+  const int nlow = ntr, nhigh = kPl - (nband - ntr);  // non-band rows [nlow, nhigh)
   const float inb = 1.f / (float)nband;
-  C* Zr = Z + ((size_t)s * n2 + z) * nrods;
-  const T* vz = v + (size_t)z * kPlane;
-  pl_backward_to_last<T>(Pl, Zr, nrods, row_rod, row_xb, nband);
-  // 8-point items: backward, v(r) product, forward, in registers
-  for (int it = threadIdx.x; it < kPl * 15; it += blockDim.x) {
-    const int j = it / kPl, x = it - j * kPl;
-    int i[8];
-    pl_slots<2>(j, i);
-    T vv[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) vv[k] = vz[i[k] * kPl + x];
-    C w[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) w[k] = Pl[i[k] * kPlLs + x];
-    pl_dft<2, +1>(w);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      w[k].x = w[k].x * vv[k];
-      w[k].y = w[k].y * vv[k];
+  C* Sg = Pl + nlow * kPlLs;  // staging: the Z row in rod order
+  const int W = n2 * ns;
+  int w = blockIdx.x;
+  if (STAGE && w < W) {
+    const C* Zr = Z + (size_t)w * nrods;
+    for (int q = threadIdx.x; q < nrods; q += blockDim.x) pl_cp16(Sg + q, Zr + q);
+    pl_cp_commit();
+  }
+  for (; w < W; w += gridDim.x) {
+    const int z = w % n2;
+    C* Zr = Z + (size_t)w * nrods;  // Z[s][z][rod] with w = z + n2 s
+    const T* vz = v + (size_t)z * kPlane;
+    if constexpr (STAGE) {
+      const C zero = pl_zero<T>();
+      for (int i = threadIdx.x; i < nband * kPlLs; i += blockDim.x) {
+        const int b = i / kPlLs;
+        Pl[(b < ntr ? i : i + (nhigh - nlow) * kPlLs)] = zero;
+      }
+      pl_cp_wait_all();
+      __syncthreads();
+      for (int q = threadIdx.x; q < nrods; q += blockDim.x) {
+        const int xb = row_xb[q];
+        const int b = xb >> 16, y = b < ntr ? b : b + (kPl - nband);
+        Pl[y * kPlLs + (xb & 0xffff)] = Sg[row_rod[q]];
+      }
+      __syncthreads();
+      // the non-band rows are zeroed alongside the first x pass, which does
+      // not touch them
+      for (int i = threadIdx.x; i < (nhigh - nlow) * kPlLs; i += blockDim.x) Sg[i] = zero;
+      pl_rows<0, +1>(Pl, nband, ntr, inb);
+      pl_rows<1, +1>(Pl, nband, ntr, inb);
+      pl_rows<2, +1>(Pl, nband, ntr, inb);
+      pl_cols<0, +1>(Pl);
+      pl_cols<1, +1>(Pl);
+    } else {
+      pl_backward_to_last<T>(Pl, Zr, nrods, row_rod, row_xb, nband);
     }
-    pl_dft<2, -1>(w);
+    // 8-point items: backward, v(r) product, forward, in registers
+    for (int it = threadIdx.x; it < kPl * 15; it += blockDim.x) {
+      const int j = it / kPl, x = it - j * kPl;
+      int i[8];
+      pl_slots<2>(j, i);
+      T vv[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) Pl[i[k] * kPlLs + x] = w[k];
+      for (int k = 0; k < 8; ++k) vv[k] = vz[i[k] * kPl + x];
+      C u[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) u[k] = Pl[i[k] * kPlLs + x];
+      pl_dft<2, +1>(u);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        u[k].x = u[k].x * vv[k];
+        u[k].y = u[k].y * vv[k];
+      }
+      pl_dft<2, -1>(u);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) Pl[i[k] * kPlLs + x] = u[k];
+    }
+    __syncthreads();
+    pl_cols<1, -1>(Pl);
+    pl_cols<0, -1>(Pl);
+    // the non-band rows are free from here on: stage the next item's Z row
+    const int wn = w + gridDim.x;
+    if (STAGE && wn < W) {
+      const C* Zn = Z + (size_t)wn * nrods;
+      for (int q = threadIdx.x; q < nrods; q += blockDim.x) pl_cp16(Sg + q, Zn + q);
+      pl_cp_commit();
+    }
+    pl_rows_all<-1>(Pl, nband, ntr, inb);
+    for (int q = threadIdx.x; q < nrods; q += blockDim.x) {
+      const int xb = row_xb[q];
+      const int b = xb >> 16, y = b < ntr ? b : b + (kPl - nband);
+      Zr[row_rod[q]] = Pl[y * kPlLs + (xb & 0xffff)];
+    }
+    __syncthreads();  // the band rows are read above before the next fill
   }
-  __syncthreads();
-  pl_cols<1, -1>(Pl);
-  pl_cols<0, -1>(Pl);
-  pl_rows_all<-1>(Pl, nband, ntr, inb);
-  for (int q = threadIdx.x; q < nrods; q += blockDim.x) {
-    const int xb = row_xb[q];
-    const int b = xb >> 16, y = b < ntr ? b : b + (kPl - nband);
-    Zr[row_rod[q]] = Pl[y * kPlLs + (xb & 0xffff)];
-  }
+  pl_cp_wait_all();
 }
 
 // Output of the last backward pass, per 8-point item of column x.
@@ -381,11 +443,27 @@ bool plane_applies(const qbg_plan* p, bool fp32) {
 
 template <typename T> qbg_status plane_vloc(qbg_plan* p, int ns, cudaStream_t st) {
   const size_t sm = plane_smem_bytes<T>();
-  QBG_CUDA(pl_prep(k_plane_vloc<T>, sm));
+  QBG_CUDA(pl_prep(k_plane_vloc<T, true>, sm));
+  QBG_CUDA(pl_prep(k_plane_vloc<T, false>, sm));
   const T* v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vrdf;
+  // one persistent CTA per SM; the Z row is staged in the non-band rows when
+  // it fits there
+  if (!p->nsm) {
+    int dev = 0;
+    QBG_CUDA(cudaGetDevice(&dev));
+    QBG_CUDA(cudaDeviceGetAttribute(&p->nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int nsm = p->nsm;
+  const int W = p->np2 * ns;
+  const bool stage = (size_t)p->nrods <= (size_t)(kPl - p->nband) * kPlLs;
+  const int grid = std::min(W, std::max(nsm, 1));
   PhaseTimer pt(p, PH_XYX_VLOC, st);
-  k_plane_vloc<T><<<dim3(p->np2, ns), kPlThreads, sm, st>>>(
-      (cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, v);
+  if (stage)
+    k_plane_vloc<T, true><<<grid, kPlThreads, sm, st>>>(
+        (cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, ns, v);
+  else
+    k_plane_vloc<T, false><<<grid, kPlThreads, sm, st>>>(
+        (cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, ns, v);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }

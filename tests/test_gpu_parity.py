@@ -181,11 +181,15 @@ def test_density_216_atom_grid(cuda, prec, tol):
 
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("mixed_df32", 1e-12)])
-def test_plane_kernel_matches_band_row_kernels(cuda, prec, tol):
+@pytest.mark.parametrize("ecut", [25.0, 35.0])
+def test_plane_kernel_matches_band_row_kernels(cuda, prec, tol, ecut):
     """On 120 x 120 planes the whole-plane kernel (fused 2), the band-row
     fused kernel (1) and the separate x, y, x kernels (0) give the same
-    H|psi> and density to the rounding of the transform arithmetic."""
-    cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=6)
+    H|psi> and density to the rounding of the transform arithmetic.  At the
+    216-atom cell's cutoff the Z row of a plane (3577 rods) is staged in the
+    plane's 52 non-band rows; at the higher cutoff (5005 rods, 40 non-band
+    rows) it does not fit and the plane fills straight from HBM."""
+    cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=6, ecut=ecut)
     occ = synth.occupations(cell)
     torch = _torch()
     p = dev(psi)
