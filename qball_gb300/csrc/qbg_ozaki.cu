@@ -495,7 +495,10 @@ __global__ void __launch_bounds__(OZ_THREADS, 1) k_oz_gemm(OzArgs args) {
         }
     } else if (warp == 1 && lane == 0) {
       // ---------------- MMA issuer
-      const uint32_t idesc = idesc_f16_f32(OZ_M, OZ_N);
+      // the last N tile multiplies only its valid rows of B (rounded up to
+      // the MMA's multiple of 16): no tensor work on padding rows
+      const uint32_t idesc =
+          idesc_f16_f32(OZ_M, min(OZ_N, (args.N - nt * OZ_N + 15) & ~15));
       int q = 0;
       uint32_t used = 0, par = 0;
       const bool ok = oz_mma<0>(args, c, idesc, nks, q, used, par) &&

@@ -342,7 +342,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_tc_gemm(TcArgs args) {
         }
     } else if (warp == 1 && lane == 0) {
       // ---------------- MMA issuer
-      const uint32_t idesc = idesc_f16_f32(TC_M, TC_N);
+      // the last N tile multiplies only its valid rows of B (rounded up to
+      // the MMA's multiple of 16): no tensor work on padding rows
+      const uint32_t idesc =
+          idesc_f16_f32(TC_M, min(TC_N, (args.N - nt * TC_N + 15) & ~15));
       int i = 0;
       for (int c = 0; c < nchunks && !*abort_flag; ++c) {
         const int b = c % TC_NBUF;
