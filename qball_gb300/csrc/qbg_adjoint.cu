@@ -74,8 +74,10 @@ struct AdjWork {
   double2* chi = nullptr;        // P_b^+ lambda
   double2* lf[4] = {};           // (D/Omega) <beta|H^j y0>, j = 0..3
   size_t lf_bytes = 0;
-  double2* fields = nullptr; size_t fields_bytes = 0;  // [8][chunk][N] real space (or the
-                                                       // whole-plane field and slots)
+  double2* fields = nullptr; size_t fields_bytes = 0;  // [8][chunk][N] real space, or
+                                                       // bwd g_j [nst][N] on whole planes
+  double* pslots = nullptr; size_t pslots_bytes = 0;   // per-state pairing slots, one chunk
+  double2* gvec = nullptr; size_t gvec_bytes = 0;      // g_j [ld x nst]
   double2* proj = nullptr; size_t proj_bytes = 0;      // [12][nst][P]
   double* part = nullptr; size_t part_bytes = 0;       // block partial sums
   double* occ = nullptr; size_t occ_bytes = 0;         // per-state occupations
@@ -95,7 +97,8 @@ struct AdjWork {
 static void work_free(AdjWork* w) {
   if (!w) return;
   void* bufs[] = {w->Y[0], w->Y[1], w->Y[2], w->Y[3], w->chi, w->lf[0], w->lf[1], w->lf[2],
-                  w->lf[3], w->fields, w->proj, w->part, w->occ, w->dbeta, w->run};
+                  w->lf[3], w->fields, w->pslots, w->gvec, w->proj, w->part, w->occ,
+                  w->dbeta, w->run};
   for (void* b : bufs)
     if (b) cudaFree(b);
   keep_free(w->one);
@@ -362,8 +365,40 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* const* x,
   taylor_coefs(tau, c);
   for (int k = 0; k <= 4; ++k) cc[k] = make_double2(c[k].x, -c[k].y);
   const double2* yv[5] = {y0, w->Y[0], w->Y[1], w->Y[2], w->Y[3]};
-  for (int j = 1; j <= 4; ++j)
-    QBG_TRY(h_apply(p, yv[j - 1], ld, w->Y[j - 1], nst, w->lf[j - 1], nullptr, zero, st));
+  const bool tr32 = p->prec != QBG_PREC_FP64 && p->prec != QBG_PREC_MIXED_FFT64 &&
+                    p->prec != QBG_PREC_MIXED_DF32;
+  // On whole planes dL/dv is formed inside the four H applications below:
+  // sum_m Re(conj(bwd M_m) bwd x_m) = sum_j Re(conj(bwd H^j y0) bwd g_j) with
+  // g_j = sum_{m <= 3-j} c_{j+m+1} x_m (M_m is linear in the H^j y0), and the
+  // H application on H^j y0 holds bwd H^j y0 (r) in registers just before
+  // its v(r) product, where it is paired with the stored field bwd g_j.
+  const bool pair_h = grad_v && plane_applies(p, tr32);
+  if (pair_h) {
+    const int ch = std::max(1, std::min(p->chunk, nst));
+    QBG_TRY(ensure((void**)&w->fields, &w->fields_bytes, sizeof(double2) * (size_t)nst * p->N));
+    QBG_TRY(ensure((void**)&w->pslots, &w->pslots_bytes, sizeof(double) * (size_t)ch * p->N));
+    QBG_TRY(ensure((void**)&w->gvec, &w->gvec_bytes, w->vec_bytes));
+  }
+  for (int j = 1; j <= 4; ++j) {
+    if (pair_h) {
+      double2 cg[4];
+      for (int m = 0; m <= 4 - j; ++m) cg[m] = c[j + m];
+      QBG_TRY(comb(p, x, cg, 5 - j, ld, p->ngw, nst, w->gvec, st));
+      QBG_TRY(p->prec == QBG_PREC_MIXED_DF32
+                  ? plane_fields<df32>(p, w->gvec, ld, nst, w->fields, st)
+                  : plane_fields<double>(p, w->gvec, ld, nst, w->fields, st));
+      p->pair_G = w->fields;
+      p->pair_slots = w->pslots;
+      p->pair_grad = grad_v;
+      p->pair_scale = 2.0 / (double)p->N;
+    }
+    const qbg_status hs =
+        h_apply(p, yv[j - 1], ld, w->Y[j - 1], nst, w->lf[j - 1], nullptr, zero, st);
+    p->pair_G = nullptr;
+    p->pair_slots = nullptr;
+    p->pair_grad = nullptr;
+    QBG_TRY(hs);
+  }
   QBG_TRY(comb(p, yv, cc, 5, ld, p->ngw, nst, y_next, st));
   if (!grad_v && !ga) return QBG_OK;
   // M_m = sum_{j<=3-m} conj(c_{j+m+1}) H^j y0 into Y[3-m] (each written after its last read)
@@ -373,18 +408,7 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* const* x,
     QBG_TRY(comb(p, yv, cm, 4 - m, ld, p->ngw, nst, w->Y[3 - m], st));
   }
   const double2* M[4] = {w->Y[3], w->Y[2], w->Y[1], w->Y[0]};
-  const bool tr32 = p->prec != QBG_PREC_FP64 && p->prec != QBG_PREC_MIXED_FFT64 &&
-                    p->prec != QBG_PREC_MIXED_DF32;
-  if (grad_v && plane_applies(p, tr32)) {
-    // whole planes: bwd(M_m) kept as one field in the transform type, the
-    // transform of x_m multiplied into per-state slots in its last pass
-    const int ch = std::max(1, std::min(p->chunk, nst));
-    QBG_TRY(ensure((void**)&w->fields, &w->fields_bytes, plane_pair_bytes(p, ch)));
-    if (p->prec == QBG_PREC_MIXED_DF32)
-      QBG_TRY(pair_grad<df32>(p, M, x, 4, ld, nst, 2.0 / (double)p->N, grad_v, w->fields, st));
-    else
-      QBG_TRY(pair_grad<double>(p, M, x, 4, ld, nst, 2.0 / (double)p->N, grad_v, w->fields, st));
-  } else if (grad_v) {
+  if (grad_v && !pair_h) {
     const int ch = std::max(1, std::min(p->chunk, nst));
     QBG_TRY(ensure((void**)&w->fields, &w->fields_bytes, sizeof(double2) * 8 * (size_t)ch * p->N));
     for (int s0 = 0; s0 < nst; s0 += ch) {

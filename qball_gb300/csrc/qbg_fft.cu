@@ -27,6 +27,10 @@ namespace qbg {
 
 constexpr int kTile = 16;     // lines per CTA
 constexpr int kThreads = 256;
+// rods per CTA of the forward z pass on 120-point lines (kThreads
+// threads): the in-place passes' 40, 24 and 15 items per line come to 5, 3
+// and 1.875 rounds per thread
+constexpr int kTileZ120 = 32;
 
 // shared-memory elements (complex T) ahead of any v tile: one line buffer
 // when the prime-factor transform runs in place, else two plus the twiddles
@@ -66,10 +70,11 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
   extern __shared__ __align__(16) unsigned char smem[];
   const int n2 = d.n, ls = n2 + 1;
   C* A = reinterpret_cast<C*>(smem);
-  C* B = A + kTile * ls;
-  const FFTLen<T> dv = stage_twiddles<T>(d, B + kTile * ls, BIGP);
-  const int r0 = blockIdx.x * kTile;
-  const int nl = min(kTile, nrods - r0);
+  constexpr int TILE = kTile;
+  C* B = A + TILE * ls;
+  const FFTLen<T> dv = stage_twiddles<T>(d, B + TILE * ls, BIGP);
+  const int r0 = blockIdx.x * TILE;
+  const int nl = min(TILE, nrods - r0);
   const double2* ps = psi + (size_t)blockIdx.y * ld;
   for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
   __syncthreads();
@@ -122,8 +127,9 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
   if constexpr (L120) pfa120_inplace_lines<+1>(A, ls, nl);
   else R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
   C* Zs = Z + (size_t)blockIdx.y * n2 * nrods;
+  const float inl = 1.f / (float)nl;
   for (int it = threadIdx.x; it < nl * n2; it += blockDim.x) {
-    const int rl = it % nl, z = it / nl;
+    const int z = fdiv(it, inl), rl = it - z * nl;
     Zs[(size_t)z * nrods + r0 + rl] = R[rl * ls + z];
   }
 }
@@ -145,10 +151,11 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
   extern __shared__ __align__(16) unsigned char smem[];
   const int n2 = d.n, ls = n2 + 1;
   C* A = reinterpret_cast<C*>(smem);
-  C* B = A + kTile * ls;
-  const FFTLen<T> dv = stage_twiddles<T>(d, B + kTile * ls, BIGP);
-  const int r0 = blockIdx.x * kTile;
-  const int nl = min(kTile, nrods - r0);
+  constexpr int TILE = L120 ? kTileZ120 : kTile;
+  C* B = A + TILE * ls;
+  const FFTLen<T> dv = stage_twiddles<T>(d, B + TILE * ls, BIGP);
+  const int r0 = blockIdx.x * TILE;
+  const int nl = min(TILE, nrods - r0);
   const int s = blockIdx.y;
   const C* Zs = Z + (size_t)s * n2 * nrods;
   {
@@ -156,13 +163,14 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
     // from HBM and the load phase is latency bound)
     constexpr int U = 8;
     const int tot = nl * n2;
+    const float inl = 1.f / (float)nl;
     for (int it0 = threadIdx.x; it0 < tot; it0 += U * blockDim.x) {
       C v[U];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int it = it0 + u * blockDim.x;
         if (it < tot) {
-          const int rl = it % nl, z = it / nl;
+          const int z = fdiv(it, inl), rl = it - z * nl;
           v[u] = Zs[(size_t)z * nrods + r0 + rl];
         }
       }
@@ -170,7 +178,7 @@ k_z_fwd(const cplx<T>* __restrict__ Z, double2* out, int ldo,
       for (int u = 0; u < U; ++u) {
         const int it = it0 + u * blockDim.x;
         if (it < tot) {
-          const int rl = it % nl, z = it / nl;
+          const int z = fdiv(it, inl), rl = it - z * nl;
           A[rl * ls + z] = v[u];
         }
       }
@@ -347,7 +355,7 @@ k_x_bwd(const cplx<T>* __restrict__ Z, cplx<T>* __restrict__ Y, int nrods,
   const C* R = fft_lines<+1, T, BIGP>(A, B, nl, ls, dv);
   C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
   for (int it = threadIdx.x; it < nl * n0; it += blockDim.x) {
-    const int bl = it / n0, x = it - bl * n0;
+    const int bl = fdiv(it, 1.f / (float)n0), x = it - bl * n0;
     Yp[(size_t)(b0 + bl) * n0 + x] = R[bl * ls + x];
   }
 }
@@ -371,7 +379,7 @@ k_x_fwd(const cplx<T>* __restrict__ Y, cplx<T>* __restrict__ Z, int nrods,
   const int s = blockIdx.y;
   const C* Yp = Y + ((size_t)s * n2 + z) * nband * n0;
   for (int it = threadIdx.x; it < nl * n0; it += blockDim.x) {
-    const int bl = it / n0, x = it - bl * n0;
+    const int bl = fdiv(it, 1.f / (float)n0), x = it - bl * n0;
     A[bl * ls + x] = Yp[(size_t)(b0 + bl) * n0 + x];
   }
   __syncthreads();
@@ -403,13 +411,14 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
   const int z = blockIdx.x / nct;
   const int x0 = (blockIdx.x % nct) * kTile;
   const int nl = min(kTile, n0 - x0);
+  const float inl = 1.f / (float)nl;
   const size_t plane = (size_t)n0 * n1;
   // v tile [n1][kTile], fetched asynchronously during the backward transform
   T* V = reinterpret_cast<T*>(A + fft_smem_elems(d, blockDim.x));
   if (MODE == Y_VLOC) {
     const T* vz = v + (size_t)z * plane;
     for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
-      const int cl = it % nl, y = it / nl;
+      const int y = fdiv(it, inl), cl = it - y * nl;
       cp_async<sizeof(T)>(V + y * kTile + cl, vz + (size_t)y * n0 + x0 + cl);
     }
     cp_async_commit();
@@ -421,7 +430,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
     if (MODE == Y_FWD_LOAD) {
       const double2* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
       for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
-        const int cl = it % nl, y = it / nl;
+        const int y = fdiv(it, inl), cl = it - y * nl;
         const double2 fv = fs[(size_t)y * n0 + x0 + cl];
         C c;
         c.x = (T)fv.x;
@@ -434,7 +443,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
       for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
       __syncthreads();
       for (int it = threadIdx.x; it < nl * nband; it += blockDim.x) {
-        const int cl = it % nl, b = it / nl;
+        const int b = fdiv(it, inl), cl = it - b * nl;
         A[cl * ls + band_y[b]] = Yp[(size_t)b * n0 + x0 + cl];
       }
       __syncthreads();
@@ -444,7 +453,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
       // each thread reads back the v elements it fetched itself
       cp_async_wait_all();
       for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
-        const int cl = it % nl, y = it / nl;
+        const int y = fdiv(it, inl), cl = it - y * nl;
         const T vv = V[y * kTile + cl];
         C c = R[cl * ls + y];
         c.x = c.x * vv;
@@ -458,7 +467,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
     if (MODE == Y_BWD_STORE) {
       double2* fs = f + (size_t)s * plane * n2 + (size_t)z * plane;
       for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
-        const int cl = it % nl, y = it / nl;
+        const int y = fdiv(it, inl), cl = it - y * nl;
         const C c = R[cl * ls + y];
         fs[(size_t)y * n0 + x0 + cl] = make_double2((double)c.x, (double)c.y);
       }
@@ -468,7 +477,7 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
       const double ws = w[s];
       double* rz = rho + (size_t)s * plane * n2 + (size_t)z * plane;
       for (int it = threadIdx.x; it < nl * n1; it += blockDim.x) {
-        const int cl = it % nl, y = it / nl;
+        const int y = fdiv(it, inl), cl = it - y * nl;
         const C c = R[cl * ls + y];
         const double re = (double)c.x, im = (double)c.y;
         const double a = ws * (re * re + im * im);
@@ -478,22 +487,35 @@ k_y(cplx<T>* __restrict__ Y, int nband, int n0, int n2,
     } else {
       // VLOC, FWD_LOAD: keep the band rows
       for (int it = threadIdx.x; it < nl * nband; it += blockDim.x) {
-        const int cl = it % nl, b = it / nl;
+        const int b = fdiv(it, inl), cl = it - b * nl;
         Yp[(size_t)b * n0 + x0 + cl] = R[cl * ls + band_y[b]];
       }
     }
   }
 }
 
-// rho[i] = sum_k slot[k][i] in slot order (deterministic), in FP64
+// rho[i] = sum_k slot[k][i] in slot order (deterministic): FP64 slots in
+// FP64, double-float slots in double-float (the FP32 pipe; GB300 runs FP64
+// at 1/72 of its rate) with one FP64 add for the stored value.  The loads
+// of eight slots are issued before their adds.
+template <typename ST> __device__ __forceinline__ double slot_f64(ST a) { return (double)a; }
+template <> __device__ __forceinline__ double slot_f64<df32>(df32 a) { return f64_from_df32(a); }
 template <typename ST>
 __global__ void __launch_bounds__(256)
 k_sum_slots(const ST* __restrict__ slots, int nslots, long long n, double* __restrict__ rho) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x) {
-    double a = (double)slots[i];
-    for (int k = 1; k < nslots; ++k) a += (double)slots[(size_t)k * n + i];
-    rho[i] = a;
+    ST a = slots[i];
+    for (int k0 = 1; k0 < nslots; k0 += 8) {
+      ST v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (k0 + u < nslots) v[u] = slots[(size_t)(k0 + u) * n + i];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (k0 + u < nslots) a = a + v[u];
+    }
+    rho[i] = slot_f64(a);
   }
 }
 
@@ -1083,8 +1105,10 @@ static qbg_status run_z_fwd_(qbg_plan* p, double2* out, int ldo, int ns, const d
   const double* kin = p->d_kpg2A;
   PhaseTimer pt(p, PH_Z_FWD, st);
   if (!BIGP && z_inplace120(p, d)) {
-    QBG_CUDA(prep(k_z_fwd<T, MODE, false, true>, sm));
-    k_z_fwd<T, MODE, false, true><<<grid, nthreads_z(d), sm, st>>>(
+    const size_t sm120 = sizeof(cplx<T>) * (size_t)kTileZ120 * (d.n + 1);
+    const dim3 grid120((p->nrods + kTileZ120 - 1) / kTileZ120, ns);
+    QBG_CUDA(prep(k_z_fwd<T, MODE, false, true>, sm120));
+    k_z_fwd<T, MODE, false, true><<<grid120, kThreads, sm120, st>>>(
         (const cplx<T>*)p->d_Z, out, ldo, p->d_rods, p->nrods, d, scale, psi, ldp, kin,
         out_init, acc, lda, fac);
   } else {
@@ -1206,7 +1230,7 @@ qbg_status local_hpsi(qbg_plan* p, const double2* psi, int ld, double2* out, int
     const int ns = std::min(ch, nst - s0);
     QBG_TRY(run_z_bwd<T>(p, psi + (size_t)s0 * ld, ld, ns, st));
     if (plane) {
-      if constexpr (!std::is_same<T, float>::value) QBG_TRY(plane_vloc<T>(p, ns, st));
+      if constexpr (!std::is_same<T, float>::value) QBG_TRY(plane_vloc<T>(p, ns, s0, st));
     } else if (G) {
       if constexpr (!std::is_same<T, float>::value) QBG_TRY(run_xyx<T>(p, ns, G, xyx_smem, st));
     } else {
@@ -1252,31 +1276,25 @@ qbg_status backward(qbg_plan* p, const double2* c, int ldc, double2* f, int nb, 
 }
 
 template <typename T>
-qbg_status pair_grad(qbg_plan* p, const double2* const* M, const double2* const* X, int nm,
-                     int ld, int nst, double scale, double* grad, void* work, cudaStream_t st) {
+qbg_status plane_fields(qbg_plan* p, const double2* c, int ld, int nst, void* F,
+                        cudaStream_t st) {
   if constexpr (std::is_same<T, float>::value) {
-    set_error("pair_grad: no whole-plane kernel for FP32 transforms");
+    set_error("plane_fields: no whole-plane kernel for FP32 transforms");
     return QBG_ERR_UNSUPPORTED;
   } else {
     const int ch = std::max(1, std::min(p->chunk, nst));
     QBG_TRY(ensure_scratch<T>(p, ch));
     for (int s0 = 0; s0 < nst; s0 += ch) {
       const int ns = std::min(ch, nst - s0);
-      for (int m = 0; m < nm; ++m) {
-        QBG_TRY(run_z_bwd<T>(p, M[m] + (size_t)s0 * ld, ld, ns, st));
-        QBG_TRY(plane_pair_field<T>(p, ns, work, st));
-        QBG_TRY(run_z_bwd<T>(p, X[m] + (size_t)s0 * ld, ld, ns, st));
-        QBG_TRY(plane_pair<T>(p, ns, work, m > 0 ? 1 : 0, st));
-      }
-      QBG_TRY(plane_pair_sum<T>(p, ns, work, scale, grad, st));
+      QBG_TRY(run_z_bwd<T>(p, c + (size_t)s0 * ld, ld, ns, st));
+      QBG_TRY(plane_pair_field<T>(p, ns, (cplx<T>*)F + (size_t)s0 * p->N, st));
     }
     return QBG_OK;
   }
 }
-template qbg_status pair_grad<double>(qbg_plan*, const double2* const*, const double2* const*,
-                                      int, int, int, double, double*, void*, cudaStream_t);
-template qbg_status pair_grad<df32>(qbg_plan*, const double2* const*, const double2* const*,
-                                    int, int, int, double, double*, void*, cudaStream_t);
+template qbg_status plane_fields<double>(qbg_plan*, const double2*, int, int, void*,
+                                         cudaStream_t);
+template qbg_status plane_fields<df32>(qbg_plan*, const double2*, int, int, void*, cudaStream_t);
 
 template <typename T>
 qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb, cudaStream_t st) {

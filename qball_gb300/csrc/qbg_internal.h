@@ -128,6 +128,13 @@ struct qbg_plan {
   bool fuse_xyx = true;         // x, y and x passes of H psi in one kernel where they fit
   bool plane_xyx = true;        // ... as the whole-plane kernel on 120 x 120 planes
   int nsm = 0;                  // SMs of the plan's device (set on first use)
+  // adjoint pairing context, set around one H application (whole planes):
+  // grad[r] += pair_scale * sum_s Re(conj(bwd psi_s(r)) G_s(r)), G [nst][N]
+  // in the transform type, pair_slots one chunk of per-state slots
+  const void* pair_G = nullptr;
+  void* pair_slots = nullptr;
+  double* pair_grad = nullptr;
+  double pair_scale = 0.0;
   int radix_order = 0;          // Stockham radix order of the length tables (factorize)
 
   // scratch (allocated lazily, grown as needed)
@@ -220,30 +227,23 @@ qbg_status forward(qbg_plan* p, double2* f, double2* c, int ldc, int nb,
 template <typename T>
 qbg_status density(qbg_plan* p, const double2* c, int ldc, int nst,
                    const double* d_w, double* rho, cudaStream_t st);
-// dL/dv(r) of the adjoint on whole planes (120 x 120, FP64 or double-float
-// transforms): grad[r] += scale * sum_s sum_{m < nm} Re(conj(bwd(M_m))
-// bwd(X_m)) over the states, work holding plane_pair_bytes(p, chunk) bytes
+// real-space fields F[s][z][y][x] = bwd(c_s)(r) in the transform type T on
+// whole planes (120 x 120, FP64 or double-float transforms), F holding
+// nst * N complex T values
 template <typename T>
-qbg_status pair_grad(qbg_plan* p, const double2* const* M, const double2* const* X, int nm,
-                     int ld, int nst, double scale, double* grad, void* work, cudaStream_t st);
+qbg_status plane_fields(qbg_plan* p, const double2* c, int ld, int nst, void* F, cudaStream_t st);
 
 // whole-plane kernels (qbg_plane.cu): 120 x 120 planes, FP64 or
 // double-float transforms, the plan's fused mode 2
 bool plane_applies(const qbg_plan* p, bool fp32);
-template <typename T> qbg_status plane_vloc(qbg_plan* p, int ns, cudaStream_t st);
+template <typename T> qbg_status plane_vloc(qbg_plan* p, int ns, int s0, cudaStream_t st);
 template <typename T>
 qbg_status plane_density(qbg_plan* p, int ns, const double* w, int acc, void* slots,
                          cudaStream_t st);
 template <typename T> qbg_status plane_field(qbg_plan* p, int ns, double2* f, cudaStream_t st);
 template <typename T>
 qbg_status plane_fwd(qbg_plan* p, int ns, const double2* f, cudaStream_t st);
-size_t plane_pair_bytes(const qbg_plan* p, int ns);
-template <typename T> qbg_status plane_pair_field(qbg_plan* p, int ns, void* work, cudaStream_t st);
-template <typename T>
-qbg_status plane_pair(qbg_plan* p, int ns, void* work, int acc, cudaStream_t st);
-template <typename T>
-qbg_status plane_pair_sum(qbg_plan* p, int ns, const void* work, double scale, double* grad,
-                          cudaStream_t st);
+template <typename T> qbg_status plane_pair_field(qbg_plan* p, int ns, void* F, cudaStream_t st);
 
 template <typename T>
 qbg_status backward_scratch(qbg_plan* p, const double2* c, int ldc, double2* f, int nb,

@@ -23,7 +23,8 @@
 // the 8-point items on either side of a pointwise product (the local
 // potential of H psi) are one register-resident item.  The 8-point items of
 // the last backward pass hand their outputs straight to memory (density,
-// real-space fields, pair products).
+// real-space fields), and in the adjoint's H applications pair the
+// backward transform with a stored field before the v(r) product.
 //
 // Shared-memory banks: rows are 121 elements apart, so 8 consecutive rows
 // at one x (row passes, rows fastest across threads) and 8 consecutive x at
@@ -162,11 +163,17 @@ __device__ __forceinline__ void pl_cp_wait_all() {
 // item's Z row is copied into the non-band rows while the x forward passes
 // of the current one run there on the band rows only, so the next plane
 // fills from shared memory instead of waiting on HBM.
-template <typename T, bool STAGE>
+//
+// With PAIR, the backward transform psi(r) that the 8-point items hold just
+// before the v(r) product is also paired with a stored real-space field:
+// slot[w][r] = Re(conj(psi(r)) G(r)) (the adjoint's dL/dv term of this
+// H application; G and the slots are [state][z][y][x] of this chunk).
+template <typename T, bool STAGE, bool PAIR>
 __global__ void __launch_bounds__(kPlThreads, 1)
 k_plane_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
              const int* __restrict__ row_xb, int nband, int n2, int ns,
-             const T* __restrict__ v) {
+             const T* __restrict__ v, const cplx<T>* __restrict__ G,
+             typename PlSlot<T>::type* __restrict__ slots) {
   using C = cplx<T>;
   extern __shared__ __align__(16) unsigned char smem[];
   C* Pl = reinterpret_cast<C*>(smem);
@@ -222,6 +229,20 @@ k_plane_vloc(cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod
 #pragma unroll
       for (int k = 0; k < 8; ++k) u[k] = Pl[i[k] * kPlLs + x];
       pl_dft<2, +1>(u);
+      if constexpr (PAIR) {
+        const cplx<T>* Gz = G + (size_t)w * kPlane;
+        typename PlSlot<T>::type* rz = slots + (size_t)w * kPlane;
+        // two halves of four keep the field loads within 80 registers
+#pragma unroll
+        for (int h = 0; h < 8; h += 4) {
+          cplx<T> g[4];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) g[k] = Gz[i[h + k] * kPl + x];
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+            rz[i[h + k] * kPl + x] = u[h + k].x * g[k].x + u[h + k].y * g[k].y;
+        }
+      }
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         u[k].x = u[k].x * vv[k];
@@ -289,33 +310,6 @@ template <typename T, typename OUT> struct PlField {
     }
   }
 };
-// Pair product: slot (+)= Re(conj(F(r)) psi(r)) with F a stored field
-template <typename T> struct PlPair {
-  using ST = typename PlSlot<T>::type;
-  const cplx<T>* fz;
-  ST* rz;
-  int accumulate;
-  __device__ __forceinline__ void operator()(const cplx<T>* u, const int* i, int x) const {
-    // two halves of four outputs keep the loads in flight within 80 registers
-#pragma unroll
-    for (int h = 0; h < 8; h += 4) {
-      cplx<T> f[4];
-      ST old[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) f[k] = fz[i[h + k] * kPl + x];
-      if (accumulate) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) old[k] = rz[i[h + k] * kPl + x];
-      }
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const T a = f[k].x * u[h + k].x + f[k].y * u[h + k].y;
-        rz[i[h + k] * kPl + x] = accumulate ? old[k] + a : a;
-      }
-    }
-  }
-};
-
 // Backward transform of one (plane z, state s) whose last pass hands each
 // 8-point item's outputs to out (a PlDensity, PlField or PlPair bound to
 // this plane and state).
@@ -357,19 +351,6 @@ k_plane_field(const cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ 
   extern __shared__ __align__(16) unsigned char smem[];
   const int z = blockIdx.x, s = blockIdx.y;
   PlField<T, OUT> out{f + ((size_t)s * n2 + z) * kPlane};
-  pl_backward<T>(reinterpret_cast<cplx<T>*>(smem), Z + ((size_t)s * n2 + z) * nrods, nrods,
-                 row_rod, row_xb, nband, out);
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kPlThreads, 1)
-k_plane_pair(const cplx<T>* __restrict__ Z, int nrods, const int* __restrict__ row_rod,
-             const int* __restrict__ row_xb, int nband, int n2, const cplx<T>* __restrict__ F,
-             typename PlSlot<T>::type* __restrict__ slots, int accumulate) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int z = blockIdx.x, s = blockIdx.y;
-  const size_t off = ((size_t)s * n2 + z) * kPlane;
-  PlPair<T> out{F + off, slots + off, accumulate};
   pl_backward<T>(reinterpret_cast<cplx<T>*>(smem), Z + ((size_t)s * n2 + z) * nrods, nrods,
                  row_rod, row_xb, nband, out);
 }
@@ -423,11 +404,21 @@ template <typename ST>
 __global__ void __launch_bounds__(256)
 k_plane_slot_sum(const ST* __restrict__ slots, int ns, long long n, double scale,
                  double* __restrict__ grad) {
+  // the sum runs in the slots' type (double-float on the FP32 pipe), the
+  // loads of eight slots issued before their adds
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n;
        r += (long long)gridDim.x * blockDim.x) {
-    double a = 0.0;
-    for (int s = 0; s < ns; ++s) a += (double)slots[(size_t)s * n + r];
-    grad[r] += scale * a;
+    ST a = slots[r];
+    for (int s0 = 1; s0 < ns; s0 += 8) {
+      ST v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (s0 + u < ns) v[u] = slots[(size_t)(s0 + u) * n + r];
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (s0 + u < ns) a = a + v[u];
+    }
+    grad[r] += scale * pl_to_f64(a);
   }
 }
 
@@ -441,10 +432,13 @@ bool plane_applies(const qbg_plan* p, bool fp32) {
          p->len[0].allow_pfa && p->len[1].allow_pfa;
 }
 
-template <typename T> qbg_status plane_vloc(qbg_plan* p, int ns, cudaStream_t st) {
+template <typename T> qbg_status plane_vloc(qbg_plan* p, int ns, int s0, cudaStream_t st) {
+  using ST = typename PlSlot<T>::type;
   const size_t sm = plane_smem_bytes<T>();
-  QBG_CUDA(pl_prep(k_plane_vloc<T, true>, sm));
-  QBG_CUDA(pl_prep(k_plane_vloc<T, false>, sm));
+  QBG_CUDA(pl_prep(k_plane_vloc<T, true, false>, sm));
+  QBG_CUDA(pl_prep(k_plane_vloc<T, false, false>, sm));
+  QBG_CUDA(pl_prep(k_plane_vloc<T, true, true>, sm));
+  QBG_CUDA(pl_prep(k_plane_vloc<T, false, true>, sm));
   const T* v = std::is_same<T, double>::value ? (const T*)p->d_vr : (const T*)p->d_vrdf;
   // one persistent CTA per SM; the Z row is staged in the non-band rows when
   // it fits there
@@ -457,14 +451,24 @@ template <typename T> qbg_status plane_vloc(qbg_plan* p, int ns, cudaStream_t st
   const int W = p->np2 * ns;
   const bool stage = (size_t)p->nrods <= (size_t)(kPl - p->nband) * kPlLs;
   const int grid = std::min(W, std::max(nsm, 1));
-  PhaseTimer pt(p, PH_XYX_VLOC, st);
-  if (stage)
-    k_plane_vloc<T, true><<<grid, kPlThreads, sm, st>>>(
-        (cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, ns, v);
-  else
-    k_plane_vloc<T, false><<<grid, kPlThreads, sm, st>>>(
-        (cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, ns, v);
-  QBG_LAUNCHED(p);
+  // the adjoint's pairing context (set around an H application)
+  const bool pair = p->pair_G != nullptr;
+  const cplx<T>* G = pair ? (const cplx<T>*)p->pair_G + (size_t)s0 * p->N : nullptr;
+  ST* slots = (ST*)p->pair_slots;
+  {
+    PhaseTimer pt(p, PH_XYX_VLOC, st);
+    auto* k = stage ? (pair ? k_plane_vloc<T, true, true> : k_plane_vloc<T, true, false>)
+                    : (pair ? k_plane_vloc<T, false, true> : k_plane_vloc<T, false, false>);
+    k<<<grid, kPlThreads, sm, st>>>((cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x,
+                                    p->nband, p->np2, ns, v, G, slots);
+    QBG_LAUNCHED(p);
+  }
+  if (pair) {
+    PhaseTimer pt(p, PH_XY_PAIR, st);
+    k_plane_slot_sum<ST><<<2 * 152 * 4, 256, 0, st>>>(slots, ns, p->N, p->pair_scale,
+                                                      p->pair_grad);
+    QBG_LAUNCHED(p);
+  }
   return QBG_OK;
 }
 
@@ -503,58 +507,25 @@ qbg_status plane_fwd(qbg_plan* p, int ns, const double2* f, cudaStream_t st) {
   return QBG_OK;
 }
 
-size_t plane_pair_bytes(const qbg_plan* p, int ns) {
-  return (size_t)ns * p->N * (sizeof(double2) + sizeof(double));
-}
-
 template <typename T>
-qbg_status plane_pair_field(qbg_plan* p, int ns, void* work, cudaStream_t st) {
+qbg_status plane_pair_field(qbg_plan* p, int ns, void* F, cudaStream_t st) {
   const size_t sm = plane_smem_bytes<T>();
   QBG_CUDA(pl_prep(k_plane_field<T, cplx<T>>, sm));
   PhaseTimer pt(p, PH_XY_PAIR, st);
   k_plane_field<T, cplx<T>><<<dim3(p->np2, ns), kPlThreads, sm, st>>>(
       (const cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2,
-      (cplx<T>*)work);
-  QBG_LAUNCHED(p);
-  return QBG_OK;
-}
-
-template <typename T>
-qbg_status plane_pair(qbg_plan* p, int ns, void* work, int acc, cudaStream_t st) {
-  using ST = typename PlSlot<T>::type;
-  const size_t sm = plane_smem_bytes<T>();
-  QBG_CUDA(pl_prep(k_plane_pair<T>, sm));
-  PhaseTimer pt(p, PH_XY_PAIR, st);
-  const cplx<T>* F = (const cplx<T>*)work;
-  ST* slots = (ST*)((char*)work + (size_t)ns * p->N * sizeof(cplx<T>));
-  k_plane_pair<T><<<dim3(p->np2, ns), kPlThreads, sm, st>>>(
-      (const cplx<T>*)p->d_Z, p->nrods, p->d_row_rod, p->d_row_x, p->nband, p->np2, F, slots,
-      acc);
-  QBG_LAUNCHED(p);
-  return QBG_OK;
-}
-
-template <typename T>
-qbg_status plane_pair_sum(qbg_plan* p, int ns, const void* work, double scale, double* grad,
-                          cudaStream_t st) {
-  using ST = typename PlSlot<T>::type;
-  const ST* slots = (const ST*)((const char*)work + (size_t)ns * p->N * sizeof(cplx<T>));
-  PhaseTimer pt(p, PH_XY_PAIR, st);
-  k_plane_slot_sum<ST><<<2 * 152 * 4, 256, 0, st>>>(slots, ns, p->N, scale, grad);
+      (cplx<T>*)F);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
 
 #define QBG_PLANE_INST(T)                                                                      \
-  template qbg_status plane_vloc<T>(qbg_plan*, int, cudaStream_t);                             \
+  template qbg_status plane_vloc<T>(qbg_plan*, int, int, cudaStream_t);                        \
   template qbg_status plane_density<T>(qbg_plan*, int, const double*, int, void*,              \
                                        cudaStream_t);                                          \
   template qbg_status plane_field<T>(qbg_plan*, int, double2*, cudaStream_t);                  \
   template qbg_status plane_fwd<T>(qbg_plan*, int, const double2*, cudaStream_t);              \
-  template qbg_status plane_pair_field<T>(qbg_plan*, int, void*, cudaStream_t);                \
-  template qbg_status plane_pair<T>(qbg_plan*, int, void*, int, cudaStream_t);                 \
-  template qbg_status plane_pair_sum<T>(qbg_plan*, int, const void*, double, double*,          \
-                                        cudaStream_t);
+  template qbg_status plane_pair_field<T>(qbg_plan*, int, void*, cudaStream_t);
 QBG_PLANE_INST(double)
 QBG_PLANE_INST(df32)
 

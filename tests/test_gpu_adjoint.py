@@ -7,8 +7,8 @@
 - dL/dv(r) and dL/d(pulse amplitudes) of a dipole loss over a laser-driven
   run agree with central finite differences of the FP64 forward (1e-6);
 - the gradients do not depend on the checkpoint interval (1e-13);
-- on 120 x 120 planes the whole-plane pair-product gradient equals the
-  eight-field path (FP64 1e-12, mixed_df32 1e-10);
+- on 120 x 120 planes the gradient paired inside the H applications equals
+  the eight-field path (FP64 1e-12, mixed_df32 1e-10);
 - the reduced-precision forms' gradients against the FP64 adjoint
   (mixed_df32 1e-8, mixed 1e-5; observed 1.2e-10 and 1.3e-7).
 """
@@ -211,12 +211,12 @@ def test_gradients_match_oracle_adjoint(cuda):
 
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-12), ("mixed_df32", 1e-10)])
 def test_whole_plane_gradient_matches_field_path(cuda, prec, tol):
-    """dL/dv(r) on the 216-atom cell's 120^3 grid through the whole-plane
-    pair-product kernel (fused mode 2: bwd(M_m) kept as one field, the
-    transform of x_m multiplied into per-state slots in its last pass)
-    against the path that stores all eight real-space fields per state
-    (fused mode 1); dL/da_k alike.  40 states: a full 32-state chunk and a
-    last chunk of 8."""
+    """dL/dv(r) on the 216-atom cell's 120^3 grid paired inside the
+    adjoint chain's H applications (fused mode 2: the whole-plane kernel
+    multiplies bwd(H^j y0)(r), formed just before its v(r) product, with the
+    stored field bwd(g_j), g_j = sum_m c_{j+m+1} x_m) against the path that
+    stores all eight real-space fields per state (fused mode 1); dL/da_k
+    alike.  40 states: a full 32-state chunk and a last chunk of 8."""
     N = 2
     ak, G = laser(N)
     dstar = ad.target_dipole(N, scale=2e-3)
