@@ -76,8 +76,8 @@ def parse():
     ap.add_argument("--dt", type=float, default=0.05)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--fp64-warmup", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--e2e-warmup", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=8)
+    ap.add_argument("--e2e-warmup", type=int, default=2)
     ap.add_argument("--cpu-states", type=int, default=16)
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--aetrs-steps", type=int, default=3,

@@ -392,9 +392,9 @@ qbg_status qbg_etrs_graph_destroy(qbg_graph* graph);
  * first, 1: odd primes first, 2: radix 4 preferred), prime-factor in-place
  * splits on/off, the fused x-y-x kernel (whole-plane, band-row, off), the
  * register lane-group y pass on/off (FP32 transforms) -- then over states
- * per transform launch
- * group in {8, 16, 32, 64}, and keep the fastest for this plan; *chosen (may
- * be NULL) receives the states per group.  Synchronises. */
+ * per transform launch group in {8, 16, 32, 64, 96, 144}, and keep the
+ * fastest for this plan; *chosen (may be NULL) receives the states per
+ * group.  Synchronises. */
 qbg_status qbg_plan_autotune(qbg_plan* plan, const double* psi, int ld, int nst,
                              const double* occ, void* stream, int* chosen);
 

@@ -206,7 +206,7 @@ class FourierTransform:
         _check(lib().qbg_plan_create(ctypes.byref(d), int(np0), int(np1), int(np2), prec,
                                      ctypes.byref(h)), "qbg_plan_create")
         self.h = h
-        self.chunk = 32  # plan default
+        self.chunk = self.transform_config()["chunk"]  # plan default: 96 on 120 x 120 planes, else 32
         self.fp64_gemm, self.oz_slices = "ozaki", 7  # plan default
 
     def close(self):

@@ -228,7 +228,7 @@ qbg_status qbg_plan_autotune(qbg_plan* p, const double* psi, int ld, int nst, co
   // 2) states per transform launch group with that shape
   int best_ch = cfg0[0];
   best_ms = 1e30f;
-  for (int ch : {8, 16, 32, 64}) {
+  for (int ch : {8, 16, 32, 64, 96, 144}) {
     if (s != QBG_OK || (ch > 2 * nst && ch != 8)) break;
     p->chunk = ch;
     float ms = 0.f;

@@ -221,6 +221,7 @@ def test_whole_plane_gradient_matches_field_path(cuda, prec, tol):
     ak, G = laser(N)
     dstar = ad.target_dipole(N, scale=2e-3)
     cell, H, v, psi, occ = setup("c2", prec, natoms=8, nst=40)
+    H.set_chunk(32)
     res = {}
     for fused in (1, 2):
         H.set_transform_config(0, 1, fused, 1)

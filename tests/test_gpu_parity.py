@@ -156,6 +156,7 @@ def test_hpsi_216_atom_grid_full_chunk(cuda, prec, tol):
     32-state transform chunk plus a last chunk of 8, the tensor-core GEMM1
     split over K, and E_nl."""
     cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=40)
+    H.set_chunk(32)
     occ = synth.occupations(cell)
     torch = _torch()
     out = torch.zeros_like(dev(psi))
@@ -171,6 +172,7 @@ def test_density_216_atom_grid(cuda, prec, tol):
     x and y transforms of a plane and w |psi(r)|^2 in one CTA) against the
     oracle, 40 states: a full 32-state chunk and an accumulating chunk of 8."""
     cell, b, H, oft, oh, psi = setup("c2", prec=prec, natoms=8, nst=40)
+    H.set_chunk(32)
     occ = synth.occupations(cell)
     torch = _torch()
     rho = torch.zeros(oft.n012, dtype=torch.float64, device=cuda)
