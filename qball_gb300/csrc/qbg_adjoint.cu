@@ -140,20 +140,37 @@ static qbg_status work_vectors(qbg_plan* p, AdjWork* w, size_t bytes, int nst) {
 struct Comb {
   const double2* in[5];
   double2 c[5];
+  int kind[5];  // 1: c real, 2: c imaginary, 0: general
   int n;
 };
 
-// out[s][g] = sum_k c_k in_k[s][g]
+// out[s][g] = sum_k c_k in_k[s][g].  The Taylor coefficients (-i tau)^k / k!
+// are real or imaginary, so most terms cost two FP64 FMAs instead of four
+// (GB300 runs FP64 at 1/72 of FP32: these sums are FP64-bound).
 __global__ void k_comb(Comb cb, int ld, int ngw, double2* __restrict__ out) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   const int s = blockIdx.y;
   if (g >= ngw) return;
   const size_t o = (size_t)s * ld + g;
+  double2 v[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k)
+    if (k < cb.n) v[k] = cb.in[k][o];
   double re = 0.0, im = 0.0;
-  for (int k = 0; k < cb.n; ++k) {
-    const double2 v = cb.in[k][o];
-    re += cb.c[k].x * v.x - cb.c[k].y * v.y;
-    im += cb.c[k].x * v.y + cb.c[k].y * v.x;
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    if (k >= cb.n) break;
+    const double2 c = cb.c[k];
+    if (cb.kind[k] == 1) {
+      re = fma(c.x, v[k].x, re);
+      im = fma(c.x, v[k].y, im);
+    } else if (cb.kind[k] == 2) {
+      re = fma(-c.y, v[k].y, re);
+      im = fma(c.y, v[k].x, im);
+    } else {
+      re += c.x * v[k].x - c.y * v[k].y;
+      im += c.x * v[k].y + c.y * v[k].x;
+    }
   }
   out[o] = make_double2(re, im);
 }
@@ -299,6 +316,7 @@ static qbg_status comb(qbg_plan* p, const double2* const* in, const double2* c, 
   for (int k = 0; k < 5; ++k) {
     cb.in[k] = k < n ? in[k] : nullptr;
     cb.c[k] = k < n ? c[k] : make_double2(0.0, 0.0);
+    cb.kind[k] = cb.c[k].y == 0.0 ? 1 : (cb.c[k].x == 0.0 ? 2 : 0);
   }
   cb.n = n;
   k_comb<<<dim3((cnt + 255) / 256, nrows), 256, 0, st>>>(cb, ld, cnt, out);
@@ -451,14 +469,21 @@ static qbg_status adj_factor(qbg_plan* p, AdjWork* w, const double2* const* x,
         for (int j = 0; j <= 3 - m; ++j) cm[j] = cc[j + m + 1];
         double2* bM = w->proj + (size_t)m * total;
         QBG_TRY(comb(p, lf, cm, 4 - m, P, P, nst, bM, st));
-        double2* dM = w->proj + (size_t)(4 + m) * total;
-        double2* dX = w->proj + (size_t)(8 + m) * total;
-        QBG_TRY(project(p, w, true, M[m], ld, nst, dM, st));
-        QBG_TRY(project(p, w, true, x[m], ld, nst, dX, st));
         t.bM[m] = bM;
         t.bX[m] = xf[m];
-        t.dM[m] = dM;
-        t.dX[m] = dX;
+        t.dM[m] = w->proj + (size_t)(4 + m) * total;
+        t.dX[m] = w->proj + (size_t)(8 + m) * total;
+      }
+      // <beta'|M_m> and <beta'|H^m x0>: on the tensor cores the eight blocks
+      // of states go through one GEMM (stacked rows fill its N tiles)
+      if (uses_tc(p)) {
+        const double2* v8[8] = {M[0], M[1], M[2], M[3], x[0], x[1], x[2], x[3]};
+        QBG_TRY(tc_project_multi(p, w->dproj, v8, 8, ld, nst, w->proj + 4 * total, st));
+      } else {
+        for (int m = 0; m < 4; ++m) {
+          QBG_TRY(project(p, w, true, M[m], ld, nst, w->proj + (size_t)(4 + m) * total, st));
+          QBG_TRY(project(p, w, true, x[m], ld, nst, w->proj + (size_t)(8 + m) * total, st));
+        }
       }
       k_grad_nl<<<(unsigned)nnl, 256, 0, st>>>(t, total, w->part);
       QBG_LAUNCHED(p);

@@ -302,6 +302,8 @@ qbg_status tc_proj_build(qbg_plan* p, const double2* table, void** out, cudaStre
 void tc_proj_free(void* proj);
 qbg_status tc_project(qbg_plan* p, const void* proj, const double2* x, int ld, int nst,
                       double2* f, cudaStream_t st);
+qbg_status tc_project_multi(qbg_plan* p, const void* proj, const double2* const* xs, int nvec,
+                            int ld, int nst, double2* f, cudaStream_t st);
 void adj_release(qbg_plan* p);
 
 // Hartree + xc (qbg_hxc.cu): v_r from rho (device), energies stay on the

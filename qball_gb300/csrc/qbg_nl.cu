@@ -490,54 +490,62 @@ template qbg_status nl_apply<double>(qbg_plan*, const double2*, int, double2*, i
 // harmonic: 1, q_m, the five quadratics), so with dq/da = -e
 //   dbeta = -kappa exp(-i q.tau) (e.grad t - i (e.tau) t),
 //   e.grad t = s_l (e.grad P - rc^2 P (e.q)) exp(-|q|^2 rc^2 / 2).
-__global__ void k_anl_da(const double* __restrict__ kpgx, const double* __restrict__ kpg2A,
-                         int ngw, double A0, double A1, double A2, double e0, double e1,
-                         double e2, const AtomDesc* __restrict__ ad,
-                         const ProjDesc* __restrict__ pd, double2* __restrict__ dbeta) {
+__global__ void __launch_bounds__(256)
+k_anl_da(const double* __restrict__ kpgx, const double* __restrict__ kpg2A, int ngw, double A0,
+         double A1, double A2, double e0, double e1, double e2, int natoms,
+         const AtomDesc* __restrict__ ad, const ProjDesc* __restrict__ pd,
+         double2* __restrict__ dbeta) {
+  // one thread per G for all atoms: the Y_lm factors and their derivatives
+  // along e depend on q = k+G-A only and the radial Gaussian on |q| and the
+  // atom's rc (recomputed only when rc changes); per atom the structure
+  // phase and the projectors' products remain
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= ngw) return;
-  const AtomDesc at = ad[blockIdx.y];
   const double qx = kpgx[g] - A0, qy = kpgx[ngw + g] - A1, qz = kpgx[2 * ngw + g] - A2;
-  const double rc2 = at.rc * at.rc;
-  const double E = exp(-0.5 * kpg2A[g] * rc2);
+  const double k2 = kpg2A[g];
   const double eq = e0 * qx + e1 * qy + e2 * qz;
   const double fpi = 4.0 * 3.14159265358979323846;
-  const double etau = e0 * at.tau[0] + e1 * at.tau[1] + e2 * at.tau[2];
-  double sn, cs;
-  sincos(-(at.tau[0] * qx + at.tau[1] * qy + at.tau[2] * qz), &sn, &cs);
-  for (int ipr = 0; ipr < at.npr; ++ipr) {
-    const int p = at.p0 + ipr * at.stride;
-    const ProjDesc d = pd[p];
-    double P, eP, s;
-    if (d.l == 0) {
-      s = sqrt(1.0 / fpi);
-      P = 1.0;
-      eP = 0.0;
-    } else if (d.l == 1) {
-      s = sqrt(3.0 / fpi);
-      P = d.m == 0 ? qx : (d.m == 1 ? qy : qz);
-      eP = d.m == 0 ? e0 : (d.m == 1 ? e1 : e2);
-    } else {
-      const double s3 = sqrt(3.0);
-      s = sqrt(5.0 / fpi);
-      switch (d.m) {
-        case 0: P = 0.5 * (2.0 * qz * qz - qx * qx - qy * qy);
-                eP = -e0 * qx - e1 * qy + 2.0 * e2 * qz; break;
-        case 1: P = 0.5 * s3 * (qx * qx - qy * qy); eP = s3 * (e0 * qx - e1 * qy); break;
-        case 2: P = s3 * qx * qy; eP = s3 * (e0 * qy + e1 * qx); break;
-        case 3: P = s3 * qy * qz; eP = s3 * (e1 * qz + e2 * qy); break;
-        default: P = s3 * qx * qz; eP = s3 * (e0 * qz + e2 * qx); break;
-      }
+  const double s3 = sqrt(3.0);
+  // (P, eP) of the projector types, index 0 (l = 0), 1 + m (l = 1), 4 + m
+  // (l >= 2, m >= 4 sharing the last form)
+  const double S0 = sqrt(1.0 / fpi), S1 = sqrt(3.0 / fpi), S2 = sqrt(5.0 / fpi);
+  double P[9], eP[9];
+  P[0] = 1.0; eP[0] = 0.0;
+  P[1] = qx; eP[1] = e0;
+  P[2] = qy; eP[2] = e1;
+  P[3] = qz; eP[3] = e2;
+  P[4] = 0.5 * (2.0 * qz * qz - qx * qx - qy * qy);
+  eP[4] = -e0 * qx - e1 * qy + 2.0 * e2 * qz;
+  P[5] = 0.5 * s3 * (qx * qx - qy * qy); eP[5] = s3 * (e0 * qx - e1 * qy);
+  P[6] = s3 * qx * qy; eP[6] = s3 * (e0 * qy + e1 * qx);
+  P[7] = s3 * qy * qz; eP[7] = s3 * (e1 * qz + e2 * qy);
+  P[8] = s3 * qx * qz; eP[8] = s3 * (e0 * qz + e2 * qx);
+  double rc_prev = -1.0, rc2 = 0.0, E = 0.0;
+  for (int ia = 0; ia < natoms; ++ia) {
+    const AtomDesc at = ad[ia];
+    if (at.rc != rc_prev) {
+      rc_prev = at.rc;
+      rc2 = at.rc * at.rc;
+      E = exp(-0.5 * k2 * rc2);
     }
-    const double t = s * P * E;
-    const double wr = s * E * (eP - rc2 * P * eq);
-    const double wi = -etau * t;
-    const double zr = cs * wr - sn * wi, zi = sn * wr + cs * wi;
-    double2 o;
-    if (d.l == 0) o = make_double2(-zr, -zi);
-    else if (d.l == 1) o = make_double2(-zi, zr);
-    else o = make_double2(zr, zi);
-    dbeta[(size_t)p * ngw + g] = o;
+    const double etau = e0 * at.tau[0] + e1 * at.tau[1] + e2 * at.tau[2];
+    double sn, cs;
+    sincos(-(at.tau[0] * qx + at.tau[1] * qy + at.tau[2] * qz), &sn, &cs);
+    for (int ipr = 0; ipr < at.npr; ++ipr) {
+      const int p = at.p0 + ipr * at.stride;
+      const int l = pd[p].l, m = pd[p].m;
+      const int lm = l == 0 ? 0 : (l == 1 ? 1 + m : 4 + min(m, 4));
+      const double sl = l == 0 ? S0 : (l == 1 ? S1 : S2);
+      const double t = sl * P[lm] * E;
+      const double wr = sl * E * (eP[lm] - rc2 * P[lm] * eq);
+      const double wi = -etau * t;
+      const double zr = cs * wr - sn * wi, zi = sn * wr + cs * wi;
+      double2 o;
+      if (l == 0) o = make_double2(-zr, -zi);
+      else if (l == 1) o = make_double2(-zi, zr);
+      else o = make_double2(zr, zi);
+      dbeta[(size_t)p * ngw + g] = o;
+    }
   }
 }
 
@@ -552,10 +560,9 @@ qbg_status nl_build_da(qbg_plan* p, const double* e, double2* dbeta, cudaStream_
     set_error("projector derivative: the projector table is not built");
     return QBG_ERR_STATE;
   }
-  dim3 grid((p->ngw + 255) / 256, (unsigned)p->nl_natoms);
-  k_anl_da<<<grid, 256, 0, st>>>(p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2], e[0],
-                                 e[1], e[2], (const AtomDesc*)p->d_adesc,
-                                 (const ProjDesc*)p->d_pdesc, dbeta);
+  k_anl_da<<<(p->ngw + 255) / 256, 256, 0, st>>>(
+      p->d_kpgx, p->d_kpg2A, p->ngw, p->A[0], p->A[1], p->A[2], e[0], e[1], e[2], p->nl_natoms,
+      (const AtomDesc*)p->d_adesc, (const ProjDesc*)p->d_pdesc, dbeta);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }

@@ -218,9 +218,11 @@ __global__ void k_rowmax_c64(const double2* __restrict__ x, int ld, int ncols,
 // layout per piece) per thread, so every store fills whole sectors
 __global__ void k_split_rows4(const double2* __restrict__ x, int ld, int ncols,
                               const double* __restrict__ rmax, __half* __restrict__ Y,
-                              int nRT, int nKS, float* __restrict__ rscale) {
+                              int nRT, int nKS, float* __restrict__ rscale, int n0) {
+  // row blockIdx.y of x becomes row n0 + blockIdx.y of the pieces
   const int g0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
-  const int n = blockIdx.y;
+  const int n = n0 + (int)blockIdx.y;
+  x += (size_t)blockIdx.y * ld;
   const int e = scale_exp(rmax[n]);
   if (g0 == 0) rscale[n] = ldexpf(1.f, e);
   if (g0 >= ncols) return;
@@ -236,7 +238,7 @@ __global__ void k_split_rows4(const double2* __restrict__ x, int ld, int ncols,
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     const int g = g0 + j;
-    const double2 a = g < ncols ? x[(size_t)n * ld + g] : make_double2(0.0, 0.0);
+    const double2 a = g < ncols ? x[g] : make_double2(0.0, 0.0);
     const float xr = fscale ? f32_from_f64_rn(a.x) * sf : __double2float_rn(a.x * sd);
     const float xi = fscale ? f32_from_f64_rn(a.y) * sf : __double2float_rn(a.y * sd);
     split2(xr, hi[2 * j], lo[2 * j]);
@@ -621,25 +623,31 @@ static qbg_status ensure_pieces(__half** buf, size_t* cur, size_t need, cudaStre
 }
 
 // GEMM1 of a projector table X1 (scales s1; x1_RT x x1_KS pieces of the
-// plan's layout) with the nst vectors x: split x into t->Y, leave the split-K
-// partial sums in t->part ([nsplit][nst][2P]) and return nsplit.
+// plan's layout) with the nvec blocks of nst vectors xs[k] stacked as one
+// operand of nvec * nst rows: split them into t->Y, leave the split-K partial
+// sums in t->part ([nsplit][nvec * nst][2P]) and return nsplit.
 static qbg_status tc_gemm1(qbg_plan* p, TcTables* t, const __half* X1, const float* s1,
-                           const double2* x, int ld, int nst, int* nsplit_out, cudaStream_t st) {
+                           const double2* const* xs, int nvec, int ld, int nst,
+                           int* nsplit_out, cudaStream_t st) {
   const int P = t->P, ngw = t->ngw;
-  const int nRT = (nst + TC_N - 1) / TC_N;
+  const int nrows = nvec * nst;
+  const int nRT = (nrows + TC_N - 1) / TC_N;
   QBG_TRY_TC(ensure_pieces(&t->Y, &t->Y_bytes, pieces_bytes(nRT, t->x1_KS), st));
   QBG_TRY_TC(ensure((void**)&t->sY, &t->sY_bytes, sizeof(float) * nRT * TC_N));
   QBG_TRY_TC(ensure((void**)&t->rmax, &t->rmax_bytes, sizeof(double) * nRT * TC_N));
   {
     PhaseTimer pt(p, PH_MISC, st);
-    QBG_CUDA(cudaMemsetAsync(t->rmax, 0, sizeof(double) * nst, st));
-    k_rowmax_c64<<<dim3(std::min(32, (ngw + 255) / 256), nst), 256, 0, st>>>(x, ld, ngw,
-                                                                           t->rmax);
-    QBG_LAUNCHED(p);
-    k_split_rows4<<<dim3((ngw + 1023) / 1024, nst), 256, 0, st>>>(x, ld, ngw, t->rmax, t->Y,
-                                                                 nRT, t->x1_KS, t->sY);
-    QBG_LAUNCHED(p);
+    QBG_CUDA(cudaMemsetAsync(t->rmax, 0, sizeof(double) * nrows, st));
+    for (int k = 0; k < nvec; ++k) {
+      k_rowmax_c64<<<dim3(std::min(32, (ngw + 255) / 256), nst), 256, 0, st>>>(
+          xs[k], ld, ngw, t->rmax + (size_t)k * nst);
+      QBG_LAUNCHED(p);
+      k_split_rows4<<<dim3((ngw + 1023) / 1024, nst), 256, 0, st>>>(
+          xs[k], ld, ngw, t->rmax, t->Y, nRT, t->x1_KS, t->sY, k * nst);
+      QBG_LAUNCHED(p);
+    }
   }
+  const int nst_all = nrows;
   const int mt1 = t->x1_RT;
   // split K so that the CTAs (one per SM) fill their last wave: the time is
   // ~ waves / nsplit, waves = ceil(tiles * nsplit / SMs); at least ~3 waves
@@ -663,7 +671,7 @@ static qbg_status tc_gemm1(qbg_plan* p, TcTables* t, const __half* X1, const flo
   }
   const int ksp = (t->x1_KS + nsplit - 1) / nsplit;
   nsplit = (t->x1_KS + ksp - 1) / ksp;
-  QBG_TRY_TC(ensure((void**)&t->part, &t->part_bytes, sizeof(double) * nsplit * nst * 2 * P));
+  QBG_TRY_TC(ensure((void**)&t->part, &t->part_bytes, sizeof(double) * nsplit * nst_all * 2 * P));
   TcArgs a1;
   a1.A = X1;
   a1.B = t->Y;
@@ -671,7 +679,7 @@ static qbg_status tc_gemm1(qbg_plan* p, TcTables* t, const __half* X1, const flo
   a1.nRTb = nRT;
   a1.nKS = t->x1_KS;
   a1.M = 2 * P;
-  a1.N = nst;
+  a1.N = nst_all;
   a1.ks_per_split = ksp;
   a1.sA = s1;
   a1.sB = t->sY;
@@ -702,7 +710,7 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
   QBG_TRY_TC(ensure((void**)&t->sF, &t->sF_bytes, sizeof(float) * nRT * TC_N));
   QBG_TRY_TC(ensure((void**)&t->fnl, &t->fnl_bytes, sizeof(double2) * (size_t)P * nst));
   int nsplit = 1;
-  QBG_TRY_TC(tc_gemm1(p, t, t->X1, t->s1, psi, ld, nst, &nsplit, st));
+  QBG_TRY_TC(tc_gemm1(p, t, t->X1, t->s1, &psi, 1, ld, nst, &nsplit, st));
   const size_t total = (size_t)P * nst;
   const int rb = (int)((total + 255) / 256);
   *enl_blocks = rb;
@@ -719,7 +727,7 @@ qbg_status tc_nl_apply(qbg_plan* p, const double2* psi, int ld, double2* out, in
                                                                          t->rmax);
     QBG_LAUNCHED(p);
     k_split_rows4<<<dim3((P + 1023) / 1024, nst), 256, 0, st>>>(t->fnl, P, P, t->rmax, t->F,
-                                                               nRT, t->x2_KS, t->sF);
+                                                               nRT, t->x2_KS, t->sF, 0);
     QBG_LAUNCHED(p);
   }
   // GEMM2 writes the NL part of H psi
@@ -815,15 +823,23 @@ qbg_status tc_proj_build(qbg_plan* p, const double2* table, void** proj, cudaStr
 // weights); proj == nullptr projects on the plan's own table.
 qbg_status tc_project(qbg_plan* p, const void* proj, const double2* x, int ld, int nst,
                       double2* f, cudaStream_t st) {
+  return tc_project_multi(p, proj, &x, 1, ld, nst, f, st);
+}
+
+// nvec blocks in one GEMM (the stacked rows fill the N tiles): f holds the
+// nvec [nst][P] results one after the other
+qbg_status tc_project_multi(qbg_plan* p, const void* proj, const double2* const* xs, int nvec,
+                            int ld, int nst, double2* f, cudaStream_t st) {
   TcTables* t = (TcTables*)p->tc;
   if (!t || t->stale) QBG_TRY_TC(tc_build(p, st));
   t = (TcTables*)p->tc;
-  if (!t || nst == 0) return QBG_OK;
+  if (!t || nst == 0 || nvec == 0) return QBG_OK;
   const TcProj* q = (const TcProj*)proj;
   int nsplit = 1;
-  QBG_TRY_TC(tc_gemm1(p, t, q ? q->X1 : t->X1, q ? q->s1 : t->s1, x, ld, nst, &nsplit, st));
-  const size_t total = (size_t)t->P * nst;
-  k_tc_proj_sum<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(t->part, nsplit, t->P, nst, f);
+  QBG_TRY_TC(tc_gemm1(p, t, q ? q->X1 : t->X1, q ? q->s1 : t->s1, xs, nvec, ld, nst, &nsplit, st));
+  const int nrows = nvec * nst;
+  const size_t total = (size_t)t->P * nrows;
+  k_tc_proj_sum<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(t->part, nsplit, t->P, nrows, f);
   QBG_LAUNCHED(p);
   return QBG_OK;
 }
