@@ -597,6 +597,15 @@ def run_ours(args, rank, world, local):
         pr2 = H2.profile_read()
         H2.profile(False)
         ent["phases_ms_per_H"] = {k: round(v[0], 3) for k, v in pr2.items() if v[1]}
+        # each phase against the pipe that bounds it in this form (FP64 pipe
+        # for FP64 transforms, tensor pipe for the GEMMs)
+        model2 = phase_model(H2, cell, basis)
+        ent["phase_frac_of_peak"] = {
+            k: round(model2[k][0] * cell.nst / (v[0] / 1000.0) / 1e12 /
+                     (float(peaks.get("bf16_tflops", 1917.4)) if model2[k][1][0] == "tensor"
+                      else model2[k][1][1]), 4)
+            for k, v in pr2.items() if v[1] and k in model2}
+        ent["phase_bound"] = {k: model2[k][1][0] for k, v in pr2.items() if v[1] and k in model2}
         others[label] = ent
         del H2, p2
         torch.cuda.empty_cache()

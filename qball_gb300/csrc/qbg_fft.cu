@@ -31,6 +31,13 @@ constexpr int kThreads = 256;
 // threads): the in-place passes' 40, 24 and 15 items per line come to 5, 3
 // and 1.875 rounds per thread
 constexpr int kTileZ120 = 32;
+// rods a warp gathers at once in the backward z pass: 2 keeps the kernel
+// at 64 registers (28 resident warps per SM instead of 15 at 4 rods and
+// 110 registers); 1.54 ms per H|psi> of the 216-atom cell against 1.74
+#ifndef QBG_ZGATHER_RODS
+#define QBG_ZGATHER_RODS 2
+#endif
+constexpr int kZGather = QBG_ZGATHER_RODS;
 
 // shared-memory elements (complex T) ahead of any v tile: one line buffer
 // when the prime-factor transform runs in place, else two plus the twiddles
@@ -79,14 +86,14 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
   for (int i = threadIdx.x; i < nl * ls; i += blockDim.x) A[i] = czero<T>();
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  // a warp takes up to four rods at once and every lane issues all its loads
-  // (up to 4 x 4 coefficients) before it stores any: the gather is latency
-  // bound, so the more loads in flight the better
-  for (int rb = warp; rb < nl; rb += 4 * nw) {
-    RodInfo ri[4];
-    double2 v[4][4];
+  // a warp takes up to kZGather rods at once and every lane issues all its
+  // loads (up to 4 coefficients a rod) before it stores any: the gather is
+  // latency bound, so the more loads in flight the better
+  for (int rb = warp; rb < nl; rb += kZGather * nw) {
+    RodInfo ri[kZGather];
+    double2 v[kZGather][4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < kZGather; ++r) {
       const int rl = rb + r * nw;
       ri[r] = rl < nl ? rods[r0 + rl] : RodInfo{0, 0, 0, 0};
 #pragma unroll
@@ -96,7 +103,7 @@ k_z_bwd(const double2* __restrict__ psi, int ld, cplx<T>* __restrict__ Z,
       }
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < kZGather; ++r) {
       const int rl = rb + r * nw;
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
