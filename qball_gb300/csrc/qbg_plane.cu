@@ -38,7 +38,11 @@ namespace qbg {
 
 constexpr int kPl = 120;         // plane side
 constexpr int kPlLs = kPl + 1;   // row stride in shared memory (elements)
-constexpr int kPlThreads = 768;  // 24 warps; 80 registers per thread
+// threads per CTA: 768 = 24 warps at 80 registers per thread
+#ifndef QBG_PL_THREADS
+#define QBG_PL_THREADS 768
+#endif
+constexpr int kPlThreads = QBG_PL_THREADS;
 constexpr size_t kPlane = (size_t)kPl * kPl;
 template <typename T> constexpr size_t plane_smem_bytes() {
   return sizeof(cplx<T>) * (size_t)kPl * kPlLs;
