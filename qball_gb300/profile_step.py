@@ -32,6 +32,10 @@ def main():
     ap.add_argument("--hpsi", type=int, default=0)
     ap.add_argument("--hxc", default="on", choices=["on", "off"],
                     help="self-consistent Hartree + LDA potential in the ETRS steps")
+    ap.add_argument("--phases", action="store_true",
+                    help="after one warm-up H|psi>, time the --hpsi applications with the "
+                         "library's per-phase profiler (each launch alone) and print the mean "
+                         "ms per H of every phase as JSON; not for use under ncu")
     args = ap.parse_args()
     kw = {}
     if args.nst:
@@ -57,8 +61,18 @@ def main():
     if args.hxc == "on":
             synth.enable_selfconsistent(H, cell, psi, occ)
     out = torch.zeros_like(psi)
+    if args.phases and args.hpsi:
+        H.hpsi(psi, out, occ)
+        H.profile(True)
     for _ in range(args.hpsi):
         H.hpsi(psi, out, occ)
+    if args.phases and args.hpsi:
+        pr = H.profile_read()
+        H.profile(False)
+        import json
+        print(json.dumps({"form": args.form, "natoms": cell.natoms, "nst": cell.nst,
+                          "ms_per_H": {k: round(v[0] / args.hpsi, 3)
+                                       for k, v in pr.items() if v[1]}}))
     for _ in range(args.steps):
         H.etrs_step(psi, occ, 0.05, A_t=A, A_tdt=A)
     torch.cuda.synchronize()
