@@ -15,9 +15,12 @@
 //            or the store of the full grid (plain backward).
 // The forward direction runs the same passes in reverse and fuses the
 // sphere scatter, the 1/N scale, the kinetic term and the Taylor-series
-// accumulation into the last z pass.
-// States are processed in chunks so the Z/Y intermediates of a chunk stay
-// L2-resident between passes.
+// accumulation into the last z pass.  On 120 x 120 planes the x and y passes
+// run as one whole-plane kernel per (plane, state) item (qbg_plane.cu); the
+// band-row fused kernels below serve the 48 and 40 grids, and the separate
+// x and y passes every other grid.
+// States are processed in chunks (launch groups) that bound the Z/Y
+// intermediates.
 #include <algorithm>
 
 #include "qbg_internal.h"
